@@ -1,0 +1,357 @@
+"""Benchmark of the GB300 CLUE path (one JSON line on stdout from rank 0).
+
+Default workload: batched CLUE 2D over 4096 synthetic HGCAL-like events whose
+sizes are log-uniform in [5k, 200k] points (216M points, 3.5 GB of inputs,
+far larger than the 129 MB L2, so no flush is needed between steps).
+
+* ``value``: events/s of the batched path (one CUDA-graph replay per step),
+  inputs and outputs resident in HBM, CUDA events on the launching stream.
+* ``e2e``: the same through the C ABI with host (pinned) buffers, H2D of the
+  inputs and D2H of all five outputs inside every step.
+* ``roofline``: the dominant kernel (k_layers), timed per stage with CUDA
+  events on its stream in a second pass over the same workload; algorithmic
+  bytes = 80 B per point (the reference's four stages each streaming their
+  SoA inputs once and writing their outputs once).
+* ``plain_*``: the same kernels one event per launch sequence.
+* ``cpu_baseline``: the oracle port (a C restatement of the reference serial
+  algorithm, bit-identical to it) over all host cores on a bounded sample.
+
+``--impl reference`` times that CPU implementation alone on the same
+workload and prints the reference arm's line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "heterogeneous-clue_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "CLUE events/s & Gpoints/s, batched vs plain on 1 GB300 (bit-exact); p99 latency"
+BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
+COMPULSORY_BYTES_PER_POINT = 36
+PARAMS = (1.3, 2.0, 2.0)
+STAGES_PER_STEP = 8
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(name):
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gen_workload(args, rank):
+    from clue_gb300 import synthetic as S
+    if args.workload in ("batched", "plain"):
+        return S.uneven_batch(args.events, seed=7 + 1000 * rank)
+    raise ValueError(args.workload)
+
+
+def cpu_sample(b, n_sample):
+    import numpy as np
+    E = b["offsets"].size - 1
+    idx = np.linspace(0, E - 1, min(n_sample, E)).astype(np.int64)
+    idx = np.unique(idx)
+    parts = {k: [] for k in ("x", "y", "layer", "weight")}
+    sizes = []
+    for e in idx:
+        s, t = b["offsets"][e], b["offsets"][e + 1]
+        for k in parts:
+            parts[k].append(b[k][s:t])
+        sizes.append(t - s)
+    off = np.zeros(len(sizes) + 1, np.int64)
+    np.cumsum(sizes, out=off[1:])
+    return dict(offsets=off, **{k: np.concatenate(v) for k, v in parts.items()})
+
+
+def time_cpu(b, n_sample, threads):
+    import oracle
+    smp = cpu_sample(b, n_sample)
+    t0 = time.perf_counter()
+    oracle.clue2d_batch(smp["offsets"], smp["x"], smp["y"], smp["layer"], smp["weight"], *PARAMS,
+                        n_threads=threads)
+    dt = time.perf_counter() - t0
+    ev = smp["offsets"].size - 1
+    return dict(events=ev, points=int(smp["offsets"][-1]), seconds=dt, events_per_s=ev / dt,
+                gpoints_per_s=smp["offsets"][-1] / dt / 1e9)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    b = gen_workload(args, 0)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        time_cpu(b, max(8, args.cpu_sample // 8), threads)
+    secs, evs, pts = 0.0, 0, 0
+    for _ in range(args.steps):
+        r = time_cpu(b, args.cpu_sample, threads)
+        secs += r["seconds"]
+        evs += r["events"]
+        pts += r["points"]
+    v = evs / secs
+    sample = (f"{args.cpu_sample} events strided over the {args.events}-event workload "
+              f"({pts // max(args.steps, 1)} points) per step")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "events/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded HGCAL-like generator)",
+            "config": _config(args, b),
+            "gpoints_per_s": pts / secs / 1e9,
+            "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _config(args, b):
+    import numpy as np
+    sizes = np.diff(b["offsets"])
+    return {"workload": f"batched CLUE 2D, {args.events} events, sizes log-uniform 5k-200k points",
+            "events": int(sizes.size), "points": int(b["offsets"][-1]),
+            "points_per_event_min_mean_max": [int(sizes.min()), float(sizes.mean()), int(sizes.max())],
+            "dc": PARAMS[0], "rhoc": PARAMS[1], "outlierDeltaFactor": PARAMS[2], "layers": 100,
+            "l2": "inputs (16 B/point) larger than L2; no flush"}
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    import clue_gb300 as C
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    b = gen_workload(args, rank)
+    E = b["offsets"].size - 1
+    N = int(b["offsets"][-1])
+    stream = torch.cuda.Stream()
+    algo = C.Clusterizer(*PARAMS, budget_bytes=96 << 30, device=local, stream=stream.cuda_stream)
+    if args.tuning:
+        algo.set_tuning(**json.loads(args.tuning))
+    dev = {k: torch.from_numpy(b[k]).cuda() for k in ("x", "y", "layer", "weight")}
+    out = dict(rho=torch.empty(N, dtype=torch.float32, device="cuda"),
+               delta=torch.empty(N, dtype=torch.float32, device="cuda"),
+               nearestHigher=torch.empty(N, dtype=torch.int32, device="cuda"),
+               isSeed=torch.empty(N, dtype=torch.int32, device="cuda"),
+               clusterIndex=torch.empty(N, dtype=torch.int32, device="cuda"))
+    off = b["offsets"]
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(v):
+        if ws > 1:
+            t = torch.tensor([v], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    def run(flags):
+        algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
+
+    # ---- batched, device resident (headline value)
+    for _ in range(args.warmup):
+        run(0)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            run(0)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    algo.synchronize()
+    barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    ms_step = ms / args.steps
+    value = ws * E * args.steps / (ms / 1000.0)
+    gpts = ws * N * args.steps / (ms / 1000.0) / 1e9
+
+    # ---- per-stage times of the same workload (roofline of the dominant kernel)
+    stage_sum = {s: 0.0 for s in C.STAGES}
+    prof_steps = max(1, min(args.steps, 5))
+    for _ in range(prof_steps):
+        st = algo.profile_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out)
+        for k, v in st.items():
+            stage_sum[k] += v
+    stage_ms = {k: v / prof_steps for k, v in stage_sum.items()}
+    peak, peak_kind = _peak_hbm()
+    layers_ms = stage_ms["layers"]
+    achieved = BYTES_PER_POINT * N / (layers_ms / 1000.0) / 1e9
+    pipe_achieved = BYTES_PER_POINT * N / (ms_step / 1000.0) / 1e9
+    tr = _traffic("k_layers_traffic.json")
+    traffic = None
+    if tr and tr.get("bytes_per_point"):
+        traffic = tr["bytes_per_point"] * N
+    roofline = {"bound": "hbm", "kernel": "k_layers", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_point": BYTES_PER_POINT,
+                "pipeline_achieved": pipe_achieved, "pipeline_frac": pipe_achieved / peak,
+                "compulsory_frac": COMPULSORY_BYTES_PER_POINT * N / (ms_step / 1000.0) / 1e9 / peak}
+
+    # ---- plain: the same kernels, one event per launch sequence
+    plain = None
+    if not args.no_plain:
+        run(C.PLAIN)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        psteps = max(1, args.steps // 3)
+        p0.record(stream)
+        for _ in range(psteps):
+            run(C.PLAIN)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = max_over_ranks(p0.elapsed_time(p1))
+        plain = ws * E * psteps / (pms / 1000.0)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        del out
+        hin = {k: torch.from_numpy(b[k]).pin_memory() for k in ("x", "y", "layer", "weight")}
+        hout = dict(rho=torch.empty(N, dtype=torch.float32).pin_memory(),
+                    delta=torch.empty(N, dtype=torch.float32).pin_memory(),
+                    nearestHigher=torch.empty(N, dtype=torch.int32).pin_memory(),
+                    isSeed=torch.empty(N, dtype=torch.int32).pin_memory(),
+                    clusterIndex=torch.empty(N, dtype=torch.int32).pin_memory())
+        for _ in range(max(1, args.warmup)):
+            algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
+        dt = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": ws * E * args.steps / dt, "unit": "events/s",
+               "h2d_bytes_per_step": 16 * N + 12 * (E + 1), "d2h_bytes_per_step": 20 * N + 32,
+               "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r = time_cpu(b, args.cpu_sample, threads)
+        cpu = {"value": r["events_per_s"], "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": f"{r['events']} events strided over the workload ({r['points']} points), "
+                         f"{r['seconds']:.1f} s on {threads} threads",
+               "gpoints_per_s": r["gpoints_per_s"]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded HGCAL-like generator)",
+                "config": _config(args, b), "gpoints_per_s": gpts,
+                "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
+                "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": STAGES_PER_STEP * args.steps,
+                "tuning": algo.get_tuning()}
+        print(json.dumps(line), flush=True)
+    algo.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched"])
+    ap.add_argument("--events", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=512)
+    ap.add_argument("--tuning", default="")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,675 @@
+// CLUE 2D on GB300: the four serial stages of
+// src/serial/plugin-CLUEClusterizer/CLUEAlgoKernels.h re-designed for the GPU.
+//
+// Pipeline of one batch (events concatenated in CSR order):
+//   k_count        points per (event, layer), warp-aggregated atomics; also
+//                  notes whether every event is already grouped by layer
+//   k_layer_scan   per-event exclusive scan -> first position of each layer
+//   k_scatter      group points by (event, layer) when the input is not
+//   k_layers       persistent CTAs over the (event, layer) queue.  Per layer,
+//                  on-chip: counting sort into the reference's 5 cm tiles
+//                  (column-major, index order inside a tile), density,
+//                  nearest-higher, seed/outlier flags and pointer jumping
+//                  to each point's root
+//   k_seed_count / k_seed_chunk_scan / k_seed_rank
+//                  event-wide seed numbering in index order
+//   k_label        clusterIndex = cluster of the root seed, -1 when the
+//                  chain ends at an outlier
+//
+// Bit-exactness with the serial backend:
+//  * candidates of a query are enumerated xBin-outer, yBin-inner, index order
+//    inside a tile (CLUEAlgoKernels.h:35-44,76-85); a column-major sort key
+//    makes each column's rows one contiguous range of the sorted layer;
+//  * rho is a sequential float sum in that order, (i==j ? 1 : 0.5) * w_j,
+//    with __fmul_rn/__fadd_rn (no contraction; the file is built --fmad=false);
+//  * "sqrtf(dx*dx+dy*dy) <= d" is evaluated as "dx*dx+dy*dy <= t" with t the
+//    largest float whose correctly rounded square root is <= d, which is the
+//    same predicate because sqrt_rn is monotone;
+//  * nearest-higher keeps the reference's strict "dist < delta" on the
+//    square-rooted distance (first candidate wins a tie); the squared
+//    distance only filters candidates that cannot win;
+//  * seeds are numbered by rank in point-index order over the whole event
+//    (CLUEAlgoKernels.h:114-131) and labels follow nearestHigher chains
+//    exactly where the reference's follower stack walks (:133-152).
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "clue_internal.h"
+
+namespace clue {
+
+namespace {
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ int warp_id() { return threadIdx.x >> 5; }
+
+// LayerTilesSerial::getXBin / getYBin (src/serial/DataFormats/LayerTilesSerial.h:24-40):
+// (v - (-250)) * 0.2 in float, truncated toward zero (saturating, NaN -> 0),
+// clamped to [0, 99].
+__device__ __forceinline__ int tile_bin(float v) {
+  const int b = __float2int_rz(__fmul_rn(__fsub_rn(v, -250.f), 0.2f));
+  return min(max(b, 0), kGridCols - 1);
+}
+
+// Event of a chunk: the last e with chunk_start[e] <= c (empty events own no chunk).
+__device__ __forceinline__ int chunk_event(const int32_t* chunk_start, int n_events, int c) {
+  int lo = 0, hi = n_events;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (chunk_start[mid] <= c) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <int NT>
+__device__ __forceinline__ int block_inclusive_scan(int v, int* s_ws, int* total) {
+  constexpr int NW = NT / 32;
+  const int lane = lane_id(), warp = warp_id();
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) s_ws[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int wv = lane < NW ? s_ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, wv, o);
+      if (lane >= o) wv += t;
+    }
+    if (lane < NW) s_ws[lane] = wv;
+  }
+  __syncthreads();
+  const int res = x + (warp > 0 ? s_ws[warp - 1] : 0);
+  *total = s_ws[NW - 1];
+  __syncthreads();
+  return res;
+}
+
+// Exclusive scan of tbl[0..n) in place, tbl[n] = total.
+template <int NT>
+__device__ void block_scan_table(int32_t* tbl, int n, int* s_ws) {
+  const int per = (n + NT - 1) / NT;
+  const int beg = min((int)threadIdx.x * per, n);
+  const int end = min(beg + per, n);
+  int sum = 0;
+  for (int i = beg; i < end; ++i) sum += tbl[i];
+  int total;
+  const int incl = block_inclusive_scan<NT>(sum, s_ws, &total);
+  int run = incl - sum;
+  for (int i = beg; i < end; ++i) {
+    const int c = tbl[i];
+    tbl[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == 0) tbl[n] = total;
+  __syncthreads();
+}
+
+// Per-layer working set: sorted SoA of the layer plus the tile table.
+// On-chip for layers up to the tuned capacity, in HBM scratch beyond it.
+struct LayerStore {
+  float* x;
+  float* y;
+  float* hw;    // 0.5f * w, the reference's neighbour term
+  float* w;     // own weight, the i == j term
+  int32_t* gid; // event-local point index
+  float* rho;
+  float* delta;
+  int32_t* nh;
+  int32_t* tbl; // kTableInts: exclusive scan over key = xBin*100 + yBin
+};
+
+struct LayerIO {
+  const float* x;
+  const float* y;
+  const float* w;
+  const int32_t* gid;  // nullptr: gid = gid_base + p
+  int32_t gid_base;
+  int64_t ev_start;
+};
+
+template <int NT>
+__device__ void process_layer(const Params2D& P, const LayerStore& S, const int m, const LayerIO& in,
+                              const Batch2D& b, int* s_ws) {
+  const int tid = threadIdx.x;
+  int32_t* kkey = reinterpret_cast<int32_t*>(S.delta);  // sort key, later final slot
+  int32_t* kprov = S.nh;                                 // provisional slot in tile
+  int32_t* slot_g = reinterpret_cast<int32_t*>(S.rho);  // gid at provisional slot
+  int32_t* slot_p = reinterpret_cast<int32_t*>(S.x);    // input position at provisional slot
+
+  // -- counting sort into tiles (kernel_compute_histogram, CLUEAlgoKernels.h:18-23)
+  for (int i = tid; i < kTableInts; i += NT) S.tbl[i] = 0;
+  __syncthreads();
+  for (int p = tid; p < m; p += NT) {
+    const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
+    kkey[p] = key;
+    kprov[p] = atomicAdd(&S.tbl[key], 1);
+  }
+  __syncthreads();
+  block_scan_table<NT>(S.tbl, kTiles, s_ws);
+  for (int p = tid; p < m; p += NT) {
+    const int q = S.tbl[kkey[p]] + kprov[p];
+    slot_g[q] = in.gid ? in.gid[p] : in.gid_base + p;
+    slot_p[q] = p;
+  }
+  __syncthreads();
+  // Atomics gave an arbitrary order inside a tile; the reference appends in
+  // index order, so place each point at its gid rank within the tile.
+  for (int q = tid; q < m; q += NT) {
+    const int p = slot_p[q];
+    const int key = kkey[p];
+    const int s = S.tbl[key], e = S.tbl[key + 1];
+    const int g = slot_g[q];
+    int rank = 0;
+    for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
+    kkey[p] = s + rank;
+  }
+  __syncthreads();
+  for (int p = tid; p < m; p += NT) {
+    const int f = kkey[p];
+    const float wv = in.w[p];
+    S.x[f] = in.x[p];
+    S.y[f] = in.y[p];
+    S.w[f] = wv;
+    S.hw[f] = __fmul_rn(0.5f, wv);
+    S.gid[f] = in.gid ? in.gid[p] : in.gid_base + p;
+  }
+  __syncthreads();
+
+  // -- local density (kernel_calculate_density, CLUEAlgoKernels.h:25-55)
+  for (int q = tid; q < m; q += NT) {
+    const float xi = S.x[q], yi = S.y[q], wi = S.w[q];
+    const int bx0 = tile_bin(__fsub_rn(xi, P.dc)), bx1 = tile_bin(__fadd_rn(xi, P.dc));
+    const int by0 = tile_bin(__fsub_rn(yi, P.dc)), by1 = tile_bin(__fadd_rn(yi, P.dc));
+    float r = 0.f;
+    for (int c = bx0; c <= bx1; ++c) {
+      const int s = S.tbl[c * kGridCols + by0], e = S.tbl[c * kGridCols + by1 + 1];
+      for (int k = s; k < e; ++k) {
+        const float dx = __fsub_rn(xi, S.x[k]);
+        const float dy = __fsub_rn(yi, S.y[k]);
+        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+        if (d2 <= P.t_dc) r = __fadd_rn(r, (k == q) ? wi : S.hw[k]);
+      }
+    }
+    S.rho[q] = r;
+  }
+  __syncthreads();
+
+  // -- distance to the nearest higher (kernel_calculate_distanceToHigher, :57-106)
+  for (int q = tid; q < m; q += NT) {
+    const float xi = S.x[q], yi = S.y[q], ri = S.rho[q];
+    const int gi = S.gid[q];
+    const int bx0 = tile_bin(__fsub_rn(xi, P.dm)), bx1 = tile_bin(__fadd_rn(xi, P.dm));
+    const int by0 = tile_bin(__fsub_rn(yi, P.dm)), by1 = tile_bin(__fadd_rn(yi, P.dm));
+    float best_s = FLT_MAX, best_d2 = INFINITY;
+    int best = -1;
+    for (int c = bx0; c <= bx1; ++c) {
+      const int s = S.tbl[c * kGridCols + by0], e = S.tbl[c * kGridCols + by1 + 1];
+      for (int k = s; k < e; ++k) {
+        const float rk = S.rho[k];
+        const bool higher = (rk > ri) || (rk == ri && S.gid[k] > gi);
+        const float dx = __fsub_rn(xi, S.x[k]);
+        const float dy = __fsub_rn(yi, S.y[k]);
+        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+        if (higher && d2 <= P.t_dm && d2 < best_d2) {
+          const float sd = __fsqrt_rn(d2);
+          if (sd < best_s) {
+            best_s = sd;
+            best_d2 = d2;
+            best = k;
+          }
+        }
+      }
+    }
+    S.delta[q] = best_s;
+    S.nh[q] = best;
+  }
+  __syncthreads();
+
+  // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
+  int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
+  for (int q = tid; q < m; q += NT) {
+    const float r = S.rho[q], d = S.delta[q];
+    const int n = S.nh[q];
+    const bool seed = (d > P.dc) && (r >= P.rhoc);
+    const bool outlier = (d > P.dm) && (r < P.rhoc);
+    const int64_t o = in.ev_start + S.gid[q];
+    b.rho[o] = r;
+    b.delta[o] = d;
+    b.nh[o] = n >= 0 ? S.gid[n] : -1;
+    b.seed[o] = seed ? 1 : 0;
+    par[q] = (!seed && !outlier && n >= 0) ? n : (seed ? -2 : -3);
+  }
+  __syncthreads();
+  // -- pointer jumping along nearestHigher (replaces the follower stack, :138-152)
+  for (;;) {
+    int changed = 0;
+    for (int q = tid; q < m; q += NT) {
+      const int p = par[q];
+      if (p >= 0) {
+        const int pp = par[p];
+        if (pp >= 0) {
+          par[q] = pp;
+          changed = 1;
+        }
+      }
+    }
+    if (!__syncthreads_or(changed)) break;
+  }
+  for (int q = tid; q < m; q += NT) {
+    const int p = par[q];
+    const int root = p >= 0 ? p : q;
+    // seed roots carry their event-local index until k_seed_rank/k_label
+    b.ci[in.ev_start + S.gid[q]] = (par[root] == -2) ? S.gid[root] : -1;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ kernels
+
+__global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
+  const int c = blockIdx.x;
+  __shared__ int s_e;
+  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  __syncthreads();
+  const int e = s_e;
+  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
+  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
+  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  bool ungrouped = false;
+  for (int64_t base = i0; base < i1; base += kChunkThreads) {
+    const int64_t i = base + threadIdx.x;
+    int key = -1;
+    if (i < i1) {
+      const int l = b.layer[i];
+      if (l < 0 || l >= kLayers) {
+        atomicExch(&b.flags[kFlagError], 1);
+        ungrouped = true;
+      } else {
+        key = e * kLayers + l;
+        if (i > es && l < b.layer[i - 1]) ungrouped = true;
+      }
+    }
+    const unsigned mask = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && lane_id() == __ffs(mask) - 1) atomicAdd(&b.lcnt[key], __popc(mask));
+  }
+  if (__syncthreads_or(ungrouped) && threadIdx.x == 0) b.flags[kFlagGrouped] = 0;
+}
+
+// One warp per event: layers 4*lane .. 4*lane+3.
+__global__ void k_layer_scan(Batch2D b) {
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= b.n_events) return;
+  const int lane = lane_id();
+  int c[4];
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int l = lane * 4 + j;
+    c[j] = l < kLayers ? b.lcnt[e * kLayers + l] : 0;
+    sum += c[j];
+  }
+  int x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  int run = (int)b.offsets[e] + x - sum;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int l = lane * 4 + j;
+    if (l < kLayers) {
+      b.lstart[e * kLayers + l] = run;
+      b.cursor[e * kLayers + l] = run;
+    }
+    run += c[j];
+  }
+}
+
+__global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
+  if (b.flags[kFlagGrouped]) return;  // input already grouped by layer
+  const int c = blockIdx.x;
+  __shared__ int s_e;
+  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  __syncthreads();
+  const int e = s_e;
+  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
+  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
+  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  const unsigned lt = (1u << lane_id()) - 1u;
+  for (int64_t base = i0; base < i1; base += kChunkThreads) {
+    const int64_t i = base + threadIdx.x;
+    int key = -1;
+    if (i < i1) {
+      const int l = b.layer[i];
+      if (l >= 0 && l < kLayers) key = e * kLayers + l;
+    }
+    const unsigned mask = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(mask) - 1;
+    int pos = 0;
+    if (key >= 0 && lane_id() == leader) pos = atomicAdd(&b.cursor[key], __popc(mask));
+    pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(mask & lt);
+    if (key >= 0) {
+      b.gx[pos] = b.x[i];
+      b.gy[pos] = b.y[i];
+      b.gw[pos] = b.w[i];
+      b.gid[pos] = (int32_t)(i - es);
+    }
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ int s_item;
+  __shared__ int s_ws[33];
+  const int n_items = b.n_events * kLayers;
+  const bool grouped = b.flags[kFlagGrouped] != 0;
+  LayerStore sm;
+  sm.tbl = reinterpret_cast<int32_t*>(dsm);
+  {
+    unsigned char* p = dsm + ((kTableInts * 4 + 15) / 16) * 16;
+    sm.x = reinterpret_cast<float*>(p);
+    sm.y = sm.x + cap;
+    sm.hw = sm.y + cap;
+    sm.w = sm.hw + cap;
+    sm.gid = reinterpret_cast<int32_t*>(sm.w + cap);
+    sm.rho = reinterpret_cast<float*>(sm.gid + cap);
+    sm.delta = sm.rho + cap;
+    sm.nh = reinterpret_cast<int32_t*>(sm.delta + cap);
+  }
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(&b.flags[kFlagTicket], 1);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= n_items) break;
+    const int m = b.lcnt[item];
+    if (m == 0) continue;
+    const int e = item / kLayers;
+    const int64_t es = b.offsets[e];
+    const int start = b.lstart[item];
+    LayerIO io;
+    io.ev_start = es;
+    if (grouped) {
+      io.x = b.x + start;
+      io.y = b.y + start;
+      io.w = b.w + start;
+      io.gid = nullptr;
+      io.gid_base = (int32_t)(start - es);
+    } else {
+      io.x = b.gx + start;
+      io.y = b.gy + start;
+      io.w = b.gw + start;
+      io.gid = b.gid + start;
+      io.gid_base = 0;
+    }
+    if (m <= cap) {
+      process_layer<NT>(P, sm, m, io, b, s_ws);
+    } else {
+      LayerStore g;
+      g.x = b.sp[0] + start;
+      g.y = b.sp[1] + start;
+      g.hw = b.sp[2] + start;
+      g.w = b.sp[3] + start;
+      g.gid = reinterpret_cast<int32_t*>(b.sp[4]) + start;
+      g.rho = b.sp[5] + start;
+      g.delta = b.sp[6] + start;
+      g.nh = reinterpret_cast<int32_t*>(b.sp[7]) + start;
+      g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableInts;
+      if (threadIdx.x == 0) atomicAdd(&b.flags[kFlagSpilled], 1);
+      process_layer<NT>(P, g, m, io, b, s_ws);
+    }
+  }
+}
+
+// Seeds per event-aligned chunk.
+__global__ void __launch_bounds__(kChunkThreads) k_seed_count(Batch2D b) {
+  const int c = blockIdx.x;
+  __shared__ int s_e;
+  __shared__ int s_ws[33];
+  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  __syncthreads();
+  const int e = s_e;
+  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
+  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
+  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  int cnt = 0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kChunkThreads) cnt += b.seed[i];
+  int total;
+  block_inclusive_scan<kChunkThreads>(cnt, s_ws, &total);
+  if (threadIdx.x == 0) b.chunk_seeds[c] = total;
+}
+
+// One warp per event: exclusive scan of its chunks' seed counts.
+__global__ void k_seed_chunk_scan(Batch2D b) {
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= b.n_events) return;
+  const int lane = lane_id();
+  const int c0 = b.chunk_start[e], c1 = b.chunk_start[e + 1];
+  int run = 0;
+  for (int base = c0; base < c1; base += 32) {
+    const int c = base + lane;
+    const int v = c < c1 ? b.chunk_seeds[c] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    if (c < c1) b.chunk_base[c] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+}
+
+// Cluster id of each seed = its rank among the event's seeds in index order.
+__global__ void __launch_bounds__(kChunkThreads) k_seed_rank(Batch2D b) {
+  constexpr int PER = kChunk / kChunkThreads;
+  const int c = blockIdx.x;
+  __shared__ int s_e;
+  __shared__ int s_ws[33];
+  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  __syncthreads();
+  const int e = s_e;
+  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
+  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
+  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  const int64_t my0 = i0 + (int64_t)threadIdx.x * PER;
+  int f[PER];
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    f[j] = (my0 + j < i1) ? b.seed[my0 + j] : 0;
+    sum += f[j];
+  }
+  int total;
+  const int incl = block_inclusive_scan<kChunkThreads>(sum, s_ws, &total);
+  int run = b.chunk_base[c] + incl - sum;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    if (f[j]) b.ci[my0 + j] = run;
+    run += f[j];
+  }
+}
+
+__global__ void __launch_bounds__(kChunkThreads) k_label(Batch2D b) {
+  const int c = blockIdx.x;
+  __shared__ int s_e;
+  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  __syncthreads();
+  const int e = s_e;
+  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
+  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
+  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  const int64_t n_ev = ee - es;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kChunkThreads) {
+    if (!b.seed[i]) {
+      // v is the event-local index of the root seed (or -1); points with an
+      // invalid layer were never written, so v is range-checked
+      const int v = b.ci[i];
+      b.ci[i] = (v >= 0 && v < n_ev) ? b.ci[es + v] : -1;
+    }
+  }
+}
+
+template <int NT>
+cudaError_t launch_layers(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s) {
+  const size_t smem = layer_smem_bytes(t);
+  const int grid = layer_grid(t, b.n_events * kLayers);
+  k_layers<NT><<<grid, NT, smem, s>>>(b, p, t.layer_capacity);
+  return cudaGetLastError();
+}
+
+template <int NT>
+cudaError_t allow_max_smem(int optin) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_layers<NT>);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_layers<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)a.sharedSizeBytes);
+}
+
+}  // namespace
+
+cudaError_t prepare_clue2d_kernels(int device) {
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e != cudaSuccess) return e;
+  if ((e = allow_max_smem<256>(optin)) != cudaSuccess) return e;
+  if ((e = allow_max_smem<512>(optin)) != cudaSuccess) return e;
+  return allow_max_smem<1024>(optin);
+}
+
+float sqrt_le_threshold(float d) {
+  // P(t) = sqrtf(t) <= d is monotone over t >= 0; binary search over the
+  // ordered bit patterns of non-negative finite floats.
+  if (!(sqrtf(0.f) <= d)) return -1.f;
+  uint32_t lo = 0, hi = 0x7f7fffffu;  // P(lo) holds
+  auto val = [](uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  if (sqrtf(val(hi)) <= d) return val(hi);
+  while (hi - lo > 1) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (sqrtf(val(mid)) <= d) lo = mid; else hi = mid;
+  }
+  return val(lo);
+}
+
+Params2D make_params2d(float dc, float rhoc, float odf) {
+  Params2D p;
+  p.dc = dc;
+  p.rhoc = rhoc;
+  p.odf = odf;
+  volatile float a = odf, c = dc;
+  p.dm = a * c;
+  p.t_dc = sqrt_le_threshold(dc);
+  p.t_dm = sqrt_le_threshold(p.dm);
+  return p;
+}
+
+size_t layer_smem_bytes(const Tuning2D& t) {
+  return ((size_t)(kTableInts * 4 + 15) / 16) * 16 + (size_t)t.layer_capacity * 32;
+}
+
+int layer_grid(const Tuning2D& t, int n_items) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = t.ctas_per_sm;
+  if (per_sm <= 0) {
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const size_t need = layer_smem_bytes(t) + 1024 + 256;  // + static smem and per-CTA reserve
+    per_sm = (int)(smem_sm / need);
+    per_sm = per_sm < 1 ? 1 : per_sm;
+    const int by_threads = 2048 / t.threads;
+    per_sm = per_sm > by_threads ? by_threads : per_sm;
+  }
+  int g = sms * per_sm;
+  if (g > n_items) g = n_items;
+  return g < 1 ? 1 : g;
+}
+
+cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s,
+                          cudaEvent_t* ev) {
+  if (b.n_events <= 0 || b.n_points <= 0) return cudaSuccess;
+  cudaError_t err;
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], s);
+  };
+  err = cudaMemsetAsync(b.lcnt, 0, sizeof(int32_t) * (size_t)b.n_events * kLayers, s);
+  if (err != cudaSuccess) return err;
+  // ticket and counters restart; the error word is left to the caller so
+  // that it can accumulate over several launches
+  err = cudaMemsetAsync(b.flags + kFlagTicket, 0, sizeof(int32_t) * (kFlagCount - kFlagTicket), s);
+  if (err != cudaSuccess) return err;
+  // grouped = 1 until k_count sees a layer decrease (low byte of a zeroed word)
+  err = cudaMemsetAsync(b.flags + kFlagGrouped, 0, sizeof(int32_t), s);
+  if (err != cudaSuccess) return err;
+  err = cudaMemsetAsync(b.flags + kFlagGrouped, 1, 1, s);
+  if (err != cudaSuccess) return err;
+  const int nc = b.n_chunks;
+  const int warps_grid = (b.n_events * 32 + 255) / 256;
+  mark(0);
+  k_count<<<nc, kChunkThreads, 0, s>>>(b);
+  mark(1);
+  k_layer_scan<<<warps_grid, 256, 0, s>>>(b);
+  mark(2);
+  k_scatter<<<nc, kChunkThreads, 0, s>>>(b);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  mark(3);
+  switch (t.threads) {
+    case 256: err = launch_layers<256>(b, p, t, s); break;
+    case 1024: err = launch_layers<1024>(b, p, t, s); break;
+    default: err = launch_layers<512>(b, p, t, s); break;
+  }
+  if (err != cudaSuccess) return err;
+  mark(4);
+  k_seed_count<<<nc, kChunkThreads, 0, s>>>(b);
+  mark(5);
+  k_seed_chunk_scan<<<warps_grid, 256, 0, s>>>(b);
+  mark(6);
+  k_seed_rank<<<nc, kChunkThreads, 0, s>>>(b);
+  mark(7);
+  k_label<<<nc, kChunkThreads, 0, s>>>(b);
+  mark(8);
+  return cudaGetLastError();
+}
+
+}  // namespace clue
+
+namespace clue {
+namespace {
+
+// Order-sensitive 64-bit digest of a word array: sum of w[i] * (2i+1) * K.
+__global__ void k_digest(const uint32_t* a, int64_t n, unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (unsigned long long)a[i] * (2ull * (unsigned long long)i + 1ull) * 0x9E3779B97F4A7C15ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+}  // namespace
+
+cudaError_t launch_digest(const void* words, int64_t n_words, unsigned long long* d_out, cudaStream_t s) {
+  if (n_words <= 0) return cudaSuccess;
+  int blocks = (int)((n_words + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  k_digest<<<blocks, 256, 0, s>>>(static_cast<const uint32_t*>(words), n_words, d_out);
+  return cudaGetLastError();
+}
+
+}  // namespace clue

@@ -1,0 +1,144 @@
+// Internal declarations shared by the CUDA kernels and the host runtime.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace clue {
+
+// Tile grid of the reference (src/serial/DataFormats/LayerTilesConstants.h:7-26):
+// 100 layers, x and y in [-250, 250] cm, 5 cm tiles -> 100 x 100 per layer.
+constexpr int kLayers = 100;
+constexpr int kGridCols = 100;
+constexpr int kTiles = kGridCols * kGridCols;
+constexpr int kTableInts = kTiles + 1;
+// Points per event-aligned chunk of the streaming kernels (count, scatter, seed ranks).
+constexpr int kChunk = 4096;
+constexpr int kChunkThreads = 512;
+
+// Device-side status words of one run.
+enum FlagSlot : int { kFlagGrouped = 0, kFlagError = 1, kFlagTicket = 2, kFlagSpilled = 3, kFlagCount = 8 };
+
+struct Params2D {
+  float dc, rhoc, odf;
+  float dm;    // odf * dc, as the reference computes it (float product)
+  float t_dc;  // largest float t >= 0 with sqrtf(t) <= dc, or -1 when none
+  float t_dm;  // same for dm
+};
+
+// Host: fill Params2D from the three reference parameters.
+Params2D make_params2d(float dc, float rhoc, float odf);
+// Largest float t >= 0 with sqrtf(t) <= d (correctly rounded sqrt), or -1.
+float sqrt_le_threshold(float d);
+
+struct Tuning2D {
+  int threads = 512;
+  int layer_capacity = 4096;
+  float work_tile_cm = 0.f;
+  int ctas_per_sm = 0;
+};
+
+// Device views of one 2D batch.  All [N] arrays are in the caller's point order
+// (inputs/outputs) or in grouped-by-(event, layer) order (scratch).
+struct Batch2D {
+  int32_t n_events = 0;
+  int64_t n_points = 0;
+  int32_t n_chunks = 0;
+  const int64_t* offsets = nullptr;      // [E+1]
+  const int32_t* chunk_start = nullptr;  // [E+1] first chunk of each event
+  const float* x = nullptr;
+  const float* y = nullptr;
+  const int32_t* layer = nullptr;
+  const float* w = nullptr;
+  float* rho = nullptr;
+  float* delta = nullptr;
+  int32_t* nh = nullptr;
+  int32_t* seed = nullptr;
+  int32_t* ci = nullptr;
+  // scratch
+  int32_t* lcnt = nullptr;    // [E*100] points per (event, layer)
+  int32_t* lstart = nullptr;  // [E*100] first grouped position of (event, layer)
+  int32_t* cursor = nullptr;  // [E*100]
+  float* gx = nullptr;        // [N] grouped copies, event-local index in gid
+  float* gy = nullptr;
+  float* gw = nullptr;
+  int32_t* gid = nullptr;
+  float* sp[8] = {};          // [N] each: HBM home of layers larger than layer_capacity
+  int32_t* sp_tbl = nullptr;  // [grid * kTableInts]
+  int32_t* chunk_seeds = nullptr;  // [n_chunks]
+  int32_t* chunk_base = nullptr;   // [n_chunks]
+  int32_t* flags = nullptr;        // [kFlagCount]
+};
+
+// Grid of the layer kernel for a tuning (needs the current device).
+int layer_grid(const Tuning2D& t, int n_items);
+size_t layer_smem_bytes(const Tuning2D& t);
+
+// Opts the layer kernels into the device's full shared memory (once per
+// device, outside any stream capture).
+cudaError_t prepare_clue2d_kernels(int device);
+
+constexpr int kStages2D = 8;
+// Queues the whole 2D pipeline of one batch on `s`.  With `stage_events`
+// (kStages2D + 1 events) an event is recorded before each stage and after the last.
+cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s,
+                          cudaEvent_t* stage_events = nullptr);
+
+// Adds an order-sensitive digest of n_words 32-bit words to *d_out.
+cudaError_t launch_digest(const void* words, int64_t n_words, unsigned long long* d_out, cudaStream_t s);
+
+// ---------------------------------------------------------------- CLUE3D --
+struct Params3D {
+  int n_layers;
+  int dens_sib, nh_sib;
+  int dens_same, nh_same;
+  float dens_thr;         // density_xy_distance_sqr
+  float kdf;              // kernel_density_factor
+  float crit_xy, crit_z, crit_rho, crit_self, outlier_mult;
+  float out_thr;          // outlier_mult * crit_xy (float product)
+  // binning constants, computed on the host exactly as the reference does
+  float eta_r;            // nEtaBins / (maxEta - minEta)
+  float phi_r;            // (float)(nPhiBins * M_1_PI * 0.5f)
+  float o2pi;             // (float)(1 / (2 pi))
+  float pi_f;             // (float)M_PI
+  float twopi_f;          // (float)(2 pi)
+};
+
+struct Batch3D {
+  int32_t n_events = 0;
+  int64_t n_points = 0;
+  int32_t n_rows = 0;  // rows (layer, eta) per event: n_layers * 34 + 1
+  const int64_t* offsets = nullptr;  // [E+1]
+  const float* z = nullptr;
+  const float* eta = nullptr;
+  const float* phi = nullptr;
+  const float* roa = nullptr;
+  const float* radius = nullptr;
+  const int32_t* layer = nullptr;
+  const float* energy = nullptr;
+  const int32_t* sil = nullptr;
+  float* rho = nullptr;
+  float* delta_t = nullptr;
+  int32_t* delta_l = nullptr;
+  int32_t* nh_l = nullptr;
+  int32_t* nh_i = nullptr;
+  int32_t* seed = nullptr;
+  int32_t* ti = nullptr;
+  // scratch
+  int32_t* key = nullptr;      // [N] flat (layer, eta, phi) bin
+  int32_t* row_cnt = nullptr;  // [E * n_rows + 1]
+  int32_t* row_start = nullptr;// [E * n_rows + 1]
+  int32_t* cursor = nullptr;   // [E * n_rows]
+  int32_t* sorted = nullptr;   // [N] event-local index, by (row, phi bin, index)
+  int32_t* scol = nullptr;     // [N] phi bin of sorted entries
+  int32_t* tmp = nullptr;      // [N]
+  int32_t* par = nullptr;      // [N]
+  int32_t* ev_seeds = nullptr; // [E] tracksters per event
+  int32_t* flags = nullptr;    // [kFlagCount]
+};
+
+cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s);
+
+}  // namespace clue

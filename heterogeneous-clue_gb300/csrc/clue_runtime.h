@@ -1,0 +1,92 @@
+// Host-side runtime objects behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/clue.h"
+#include "clue_internal.h"
+
+namespace clue {
+
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+// Named, grow-only device buffers under a byte budget.  Buffers are only
+// reallocated when a request outgrows them, never per call.
+class DeviceArena {
+ public:
+  ~DeviceArena();
+  int reserve(const std::vector<size_t>& need, size_t budget);
+  void* ptr(int slot) const { return slot < (int)bufs_.size() ? bufs_[slot].p : nullptr; }
+  size_t total() const { return total_; }
+  void release();
+
+ private:
+  struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  std::vector<Buf> bufs_;
+  size_t total_ = 0;
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~PinnedBuf();
+  int reserve(size_t n);
+};
+
+// Everything a captured 2D graph bakes in.
+struct GraphKey {
+  int32_t E = -1;
+  int64_t N = -1;
+  int flags = 0;
+  int threads = 0, cap = 0, ctas = 0;
+  float work_tile = 0.f;
+  float dc = 0.f, rhoc = 0.f, odf = 0.f;
+  const void* ptrs[13] = {};
+  bool operator==(const GraphKey& o) const {
+    if (E != o.E || N != o.N || flags != o.flags || threads != o.threads || cap != o.cap || ctas != o.ctas ||
+        work_tile != o.work_tile || dc != o.dc || rhoc != o.rhoc || odf != o.odf)
+      return false;
+    for (int i = 0; i < 13; ++i)
+      if (ptrs[i] != o.ptrs[i]) return false;
+    return true;
+  }
+};
+
+size_t required_bytes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bool host_io);
+
+struct Handle {
+  int device = 0;
+  size_t budget = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t done_event = nullptr;
+  bool pending = false;
+  int error_layers = kLayers;
+  Params2D p2d{};
+  Tuning2D tuning{};
+  DeviceArena arena;
+  DeviceArena arena3d;
+  PinnedBuf stage;
+  PinnedBuf flags_host;
+  PinnedBuf nt_host;
+  cudaGraphExec_t graph_exec = nullptr;
+  GraphKey graph_key;
+
+  ~Handle();
+  int wait_previous();
+  int check_device_flags();
+  int profile_batch(int32_t E, const int64_t* off, const float* x, const float* y, const int32_t* layer,
+                    const float* w, const clue_outputs* out, float* stage_ms);
+  int run_batch(int32_t E, const int64_t* off, const float* x, const float* y, const int32_t* layer, const float* w,
+                const clue_outputs* out, int flags);
+};
+
+}  // namespace clue

@@ -1,0 +1,111 @@
+"""The oracle (CPU restatement) pinned against the reference: the golden
+vectors written by the unmodified serial code, and -- where the reference
+tree is present -- the reference itself on fresh seeded inputs."""
+import numpy as np
+import pytest
+
+import oracle
+from clue_gb300 import synthetic as S
+
+from _util import KEYS_3D, assert_bitexact, golden_2d, golden_3d, load_golden_2d, load_golden_3d
+
+needs_ref = pytest.mark.skipif(not oracle.ref_available(), reason="reference tree not present")
+
+
+@pytest.mark.parametrize("path", golden_2d(), ids=lambda p: p.split("/")[-1])
+def test_oracle_matches_golden_2d(path):
+    ev, prm, want = load_golden_2d(path)
+    got = oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *prm)
+    assert_bitexact(got, want, label=path)
+
+
+@pytest.mark.parametrize("path", golden_3d(), ids=lambda p: p.split("/")[-1])
+def test_oracle_matches_golden_3d(path):
+    ev, prm, want, nt = load_golden_3d(path)
+    got, nt2 = oracle.clue3d(ev, **prm)
+    assert nt2 == nt
+    assert_bitexact(got, want, KEYS_3D, label=path)
+
+
+@needs_ref
+@pytest.mark.parametrize("seed,prm,shuffle", [(12345, (1.3, 2.0, 2.0), False), (4, (1.3, 2.0, 2.0), True),
+                                              (5, (20.0, 25.0, 2.0), False), (6, (2.0, 3.0, 1.2), False),
+                                              (7, (0.7, 1.0, 4.0), True)])
+def test_oracle_matches_reference_toy(seed, prm, shuffle):
+    ev = S.toy_event(seed, shuffle=shuffle)
+    assert_bitexact(oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *prm),
+                    oracle.ref_clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *prm), label=str(prm))
+
+
+@needs_ref
+def test_oracle_matches_reference_hgcal():
+    ev = S.hgcal_event(1000)
+    prm = (1.3, 2.0, 2.0)
+    assert_bitexact(oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *prm),
+                    oracle.ref_clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *prm))
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [1, 2])
+@pytest.mark.parametrize("prm", [{}, dict(density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5),
+                                 dict(density_on_same_layer=1, nh_on_same_layer=1, kernel_density_factor=0.5)])
+def test_oracle_matches_reference_3d(seed, prm):
+    ev = S.clue3d_event(seed, n_layers=94)
+    got, nt = oracle.clue3d(ev, **prm)
+    want, nt2 = oracle.ref_clue3d(ev, **prm)
+    assert nt == nt2
+    assert_bitexact(got, want, KEYS_3D)
+
+
+@needs_ref
+def test_oracle_matches_reference_3d_scintillator_and_wrap():
+    """Non-silicon clusters (radius thresholds) and phi near +-pi."""
+    ev = S.clue3d_event(3, n_clusters=4000, n_layers=94)
+    rng = np.random.default_rng(0)
+    ev["isSilicon"] = (rng.random(ev["z"].size) < 0.5).astype(np.int32)
+    ev["radius"] = rng.uniform(0.5, 3.0, ev["z"].size).astype(np.float32)
+    ev["phi"][:500] = np.float32(np.pi) - rng.uniform(0, 0.05, 500).astype(np.float32)
+    ev["phi"][500:1000] = -np.float32(np.pi) + rng.uniform(0, 0.05, 500).astype(np.float32)
+    got, nt = oracle.clue3d(ev)
+    want, nt2 = oracle.ref_clue3d(ev)
+    assert nt == nt2
+    assert_bitexact(got, want, KEYS_3D)
+
+
+def test_oracle_known_answers():
+    """Hand-derived answers for a few micro cases."""
+    # one point: rho = own weight, no higher, seed iff rho >= rhoc
+    o = oracle.clue2d([1.0], [2.0], [5], [3.0], 1.3, 2.0, 2.0)
+    assert o["rho"][0] == np.float32(3.0) and o["nearestHigher"][0] == -1
+    assert o["delta"][0] == np.finfo(np.float32).max and o["isSeed"][0] == 1 and o["clusterIndex"][0] == 0
+    # two points exactly dc apart in x (1.3 is representable as the float difference below)
+    x = np.array([10.0, 11.3], np.float32)
+    d = np.float32(np.sqrt(np.float32(x[1] - x[0]) ** 2))
+    o = oracle.clue2d(x, [0.0, 0.0], [1, 1], [1.0, 1.0], float(d), 0.5, 2.0)
+    # inside dc (<=): rho = 1 + 0.5; equal rho, j > i wins: point 0 follows point 1
+    assert o["rho"].tolist() == [1.5, 1.5]
+    assert o["nearestHigher"].tolist() == [1, -1]
+    assert o["isSeed"].tolist() == [0, 1] and o["clusterIndex"].tolist() == [0, 0]
+    # a low-density point beyond odf*dc of anything is an outlier (-1)
+    o = oracle.clue2d([0.0, 0.3, 9.0], [0.0, 0.0, 0.0], [0, 0, 0], [5.0, 1.0, 0.1], 1.0, 1.0, 2.0)
+    assert o["clusterIndex"].tolist() == [0, 0, -1]
+    # layers never interact
+    o = oracle.clue2d([0.0, 0.0], [0.0, 0.0], [0, 1], [1.0, 1.0], 1.0, 0.5, 2.0)
+    assert o["isSeed"].tolist() == [1, 1] and o["clusterIndex"].tolist() == [0, 1]
+
+
+def test_oracle_rejects_bad_layer():
+    with pytest.raises(ValueError):
+        oracle.clue2d([0.0], [0.0], [100], [1.0], 1.3, 2.0, 2.0)
+
+
+def test_oracle_batch_threads_match_single():
+    b = S.uneven_batch(6, seed=3, lo=2000, hi=20000)
+    one = oracle.clue2d_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], 1.3, 2.0, 2.0, n_threads=1)
+    many = oracle.clue2d_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], 1.3, 2.0, 2.0, n_threads=4)
+    assert_bitexact(many, one)
+    e = 2
+    ev = S.event_of(b, e)
+    s, t = b["offsets"][e], b["offsets"][e + 1]
+    single = oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], 1.3, 2.0, 2.0)
+    assert_bitexact({k: v[s:t] for k, v in one.items()}, single)
