@@ -6,26 +6,6 @@ using clue::set_error;
 
 extern "C" {
 
-void clue3d_default_params(clue3d_params* p) {
-  p->n_layers = 94;
-  p->density_sibling_layers = 3;
-  p->density_xy_distance_sqr = 3.24f;
-  p->kernel_density_factor = 0.2f;
-  p->density_on_same_layer = 0;
-  p->nh_sibling_layers = 3;
-  p->nh_on_same_layer = 0;
-  p->critical_xy_distance = 1.8f;
-  p->critical_z_distance_lyr = 5.f;
-  p->critical_density = 0.6f;
-  p->critical_self_density = 0.15f;
-  p->outlier_multiplier = 2.f;
-}
-
-int clue3d_run_batch(clue_handle*, const clue3d_params*, int32_t, const int64_t*, const clue3d_inputs*,
-                     const clue3d_outputs*, int32_t*, int) {
-  return set_error(CLUE_EINVAL, "clue3d_run_batch: not available in this build");
-}
-
 int clue_server_create(const clue_params*, const clue_server_config*, clue_server**) {
   return set_error(CLUE_EINVAL, "serving: not available in this build");
 }

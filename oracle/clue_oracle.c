@@ -82,7 +82,7 @@ static int o2_ws_reserve(o2_ws *w, int64_t n) {
     w->tile_start = (int32_t *)malloc(sizeof(int32_t) * ((size_t)O2_NLAYERS * O2_NTILES + 1));
     if (!w->tile_start) return -1;
   }
-  if (n <= w->cap) return 0;
+  if (w->order && n <= w->cap) return 0;
   free(w->order);
   free(w->key);
   free(w->fstart);
@@ -399,6 +399,10 @@ static int o3_fill(o3_ws *w, int32_t n, const float *eta, const float *phi, cons
   w->stack = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n + 1));
   if (!w->tile_start || !w->order || !w->key || !w->fstart || !w->flist || !w->stack) return -3;
   for (int32_t i = 0; i < n; ++i) {
+    /* a phi that does not reduce into [-pi, pi] would index outside its
+     * layer's tiles in the reference (undefined); reject it */
+    int pb = o3_phi_bin(phi[i]);
+    if (pb < 0 || pb > O3_NPHI) return -2;
     int64_t k = o3_key(layer[i], eta[i], phi[i]);
     if (k < 0 || k >= w->nk) return -2;
     w->key[i] = k;

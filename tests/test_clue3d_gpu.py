@@ -1,0 +1,90 @@
+"""Parity of the CUDA CLUE3D path with the reference tracksterizer through
+the C ABI: bit-exact on rho, delta (transverse, layers), nearestHigher
+(layer, index), isSeed, tracksterIndex and the per-event trackster count."""
+import numpy as np
+import pytest
+
+import clue_gb300 as C
+import oracle
+from clue_gb300 import synthetic as S
+
+from _util import KEYS_3D, assert_bitexact, golden_3d, load_golden_3d
+
+pytestmark = pytest.mark.gpu
+
+GPU2ORACLE = dict(rho="rho", delta_transverse="delta_t", delta_layers="delta_l", nh_layer="nh_layer",
+                  nh_index="nh_idx", isSeed="isSeed", tracksterIndex="tracksterIndex")
+CONFIG4 = dict(n_layers=100, density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)
+
+
+@pytest.fixture(scope="module")
+def algo(cuda_lib):
+    a = C.Clusterizer(1.3, 2.0, 2.0, budget_bytes=32 << 30)
+    yield a
+    a.close()
+
+
+def _as_oracle(out, s=None, t=None):
+    return {GPU2ORACLE[k]: (v[s:t] if s is not None else v) for k, v in out.items()}
+
+
+def _oracle_batch(b, prm):
+    outs, nts = [], []
+    for e in range(b["offsets"].size - 1):
+        o, nt = oracle.clue3d(S.event3d_of(b, e), **prm)
+        outs.append(o)
+        nts.append(nt)
+    return {k: np.concatenate([o[k] for o in outs]) for k in KEYS_3D}, np.array(nts)
+
+
+@pytest.mark.parametrize("path", golden_3d(), ids=lambda p: p.split("/")[-1])
+def test_golden_vectors_3d(algo, path):
+    ev, prm, want, nt = load_golden_3d(path)
+    off = np.array([0, ev["z"].size], np.int64)
+    out, nts = algo.run_clue3d(off, ev, params=prm)
+    assert int(nts[0]) == nt
+    assert_bitexact(_as_oracle(out), want, KEYS_3D, label=path)
+
+
+@pytest.mark.parametrize("prm", [{}, CONFIG4, dict(n_layers=100, density_on_same_layer=1, nh_on_same_layer=1)])
+def test_batch_vs_oracle(algo, prm):
+    nl = prm.get("n_layers", 94)
+    b = S.clue3d_batch(8, seed0=300, n_layers=nl)
+    out, nts = algo.run_clue3d(b["offsets"], b, params=prm)
+    want, wnt = _oracle_batch(b, prm)
+    assert np.array_equal(nts, wnt)
+    assert_bitexact(_as_oracle(out), want, KEYS_3D)
+
+
+def test_device_memory_and_scintillator(algo):
+    import torch
+    b = S.clue3d_batch(5, seed0=400, n_layers=100)
+    rng = np.random.default_rng(1)
+    n = b["z"].size
+    b["isSilicon"] = (rng.random(n) < 0.5).astype(np.int32)
+    b["radius"] = rng.uniform(0.5, 3.0, n).astype(np.float32)
+    b["phi"][::7] = np.float32(np.pi)          # wrap edge: phi bin 126 lands in the next eta row
+    b["phi"][3::7] = -np.float32(np.pi)
+    b["eta"][::11] = np.float32(3.0)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(b[k])).cuda()
+           for k in ("z", "eta", "phi", "r_over_absz", "radius", "layer", "energy", "isSilicon")}
+    out = {k: torch.empty(n, dtype=torch.float32 if k in ("rho", "delta_transverse") else torch.int32,
+                          device="cuda") for k in GPU2ORACLE}
+    algo.run_clue3d(b["offsets"], dev, params=dict(n_layers=100), flags=C.DEVICE_MEMORY, out=out)
+    algo.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    want, _ = _oracle_batch(b, dict(n_layers=100))
+    assert_bitexact(_as_oracle(got), want, KEYS_3D)
+
+
+def test_bad_layer_3d(algo):
+    ev = S.clue3d_event(9, n_clusters=500, n_layers=94)
+    ev["layer"][10] = 94
+    with pytest.raises(C.ClueError) as ei:
+        algo.run_clue3d(np.array([0, 500], np.int64), ev)
+    assert ei.value.code == C.CLUE_EINVAL
+    ev["layer"][10] = 3
+    out, nt = algo.run_clue3d(np.array([0, 500], np.int64), ev)
+    want, wnt = oracle.clue3d(ev)
+    assert nt[0] == wnt
+    assert_bitexact(_as_oracle(out), want, KEYS_3D)

@@ -99,6 +99,19 @@ def test_oracle_rejects_bad_layer():
         oracle.clue2d([0.0], [0.0], [100], [1.0], 1.3, 2.0, 2.0)
 
 
+def test_oracle_empty_events():
+    """Empty events anywhere in a batch, and an empty single event."""
+    b = S.uneven_batch(3, seed=16, lo=2000, hi=5000)
+    o1, o2, o3 = b["offsets"][1:]
+    off = np.array([0, 0, o1, o1, o2, o3, o3], np.int64)
+    got = oracle.clue2d_batch(off, b["x"], b["y"], b["layer"], b["weight"], 1.3, 2.0, 2.0, n_threads=4)
+    want = oracle.clue2d_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], 1.3, 2.0, 2.0)
+    assert_bitexact(got, want)
+    e = oracle.clue2d(np.zeros(0, np.float32), np.zeros(0, np.float32), np.zeros(0, np.int32),
+                      np.zeros(0, np.float32), 1.3, 2.0, 2.0)
+    assert all(v.size == 0 for v in e.values())
+
+
 def test_oracle_batch_threads_match_single():
     b = S.uneven_batch(6, seed=3, lo=2000, hi=20000)
     one = oracle.clue2d_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], 1.3, 2.0, 2.0, n_threads=1)
