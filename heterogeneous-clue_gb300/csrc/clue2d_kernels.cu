@@ -91,38 +91,74 @@ __device__ __forceinline__ int block_inclusive_scan(int v, int* s_ws, int* total
   return res;
 }
 
-// Exclusive scan of tbl[0..n) in place, tbl[n] = total.
-template <int NT>
-__device__ void block_scan_table(int32_t* tbl, int n, int* s_ws) {
+// Exclusive scan of tbl[0..n) in place, tbl[n] = total (tbl of 16- or 32-bit counts).
+template <int NT, class TT>
+__device__ void block_scan_table(TT* tbl, int n, int* s_ws) {
   const int per = (n + NT - 1) / NT;
   const int beg = min((int)threadIdx.x * per, n);
   const int end = min(beg + per, n);
   int sum = 0;
-  for (int i = beg; i < end; ++i) sum += tbl[i];
+  for (int i = beg; i < end; ++i) sum += (int)tbl[i];
   int total;
   const int incl = block_inclusive_scan<NT>(sum, s_ws, &total);
   int run = incl - sum;
   for (int i = beg; i < end; ++i) {
-    const int c = tbl[i];
-    tbl[i] = run;
+    const int c = (int)tbl[i];
+    tbl[i] = (TT)run;
     run += c;
   }
-  if (threadIdx.x == 0) tbl[n] = total;
+  if (threadIdx.x == 0) tbl[n] = (TT)total;
   __syncthreads();
 }
 
-// Per-layer working set: sorted SoA of the layer plus the tile table.
-// On-chip for layers up to the tuned capacity, in HBM scratch beyond it.
+// Histogram increment returning the previous count.  The on-chip table holds
+// 16-bit counts (a layer there has < 65536 points), two per 32-bit word.
+__device__ __forceinline__ int hist_add(uint16_t* t, int key) {
+  unsigned* w = reinterpret_cast<unsigned*>(t) + (key >> 1);
+  const int sh = (key & 1) * 16;
+  return (int)((atomicAdd(w, 1u << sh) >> sh) & 0xffffu);
+}
+__device__ __forceinline__ int hist_add(int32_t* t, int key) { return atomicAdd(t + key, 1); }
+
+// Squared distance dx*dx + dy*dy with the reference's rounding: two
+// correctly rounded differences, two correctly rounded squares (computed as
+// one packed f32x2 pair each) and one correctly rounded sum.
+__device__ __forceinline__ float dist2(float2 a, float2 b) {
+  float sx, sy;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\t"
+      "mul.rn.f32x2 pd, pd, pd;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(sx), "=f"(sy)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return __fadd_rn(sx, sy);
+}
+
+// Order-preserving map of a non-NaN float to 32 bits (rho is never -0: it
+// starts at +0 and only adds terms).  NaN maps to 0, below every number.
+__device__ __forceinline__ unsigned float_ord(float f) {
+  const unsigned u = __float_as_uint(f);
+  if (f != f) return 0u;
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_float(unsigned o) {
+  if (o == 0u) return __uint_as_float(0x7fffffffu);  // NaN
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// Per-layer working set, sorted by tile: on-chip for layers up to the tuned
+// capacity, in HBM scratch beyond it.  32 bytes per point plus the table.
+template <class TT>
 struct LayerStore {
-  float* x;
-  float* y;
-  float* hw;    // 0.5f * w, the reference's neighbour term
-  float* w;     // own weight, the i == j term
-  int32_t* gid; // event-local point index
-  float* rho;
+  float2* xy;               // position
+  unsigned long long* key;  // (float_ord(rho) << 32) | gid; gid alone before rho exists
+  float* hw;                // 0.5f * w, the reference's neighbour term
   float* delta;
-  int32_t* nh;
-  int32_t* tbl; // kTableInts: exclusive scan over key = xBin*100 + yBin
+  int32_t* nh;              // own weight (bits) during density, then nearest higher, then parent
+  int32_t* qord;            // query order of the current phase
+  TT* tbl;                  // kTableInts: exclusive scan over key = xBin*100 + yBin
 };
 
 struct LayerIO {
@@ -134,27 +170,68 @@ struct LayerIO {
   int64_t ev_start;
 };
 
-template <int NT>
-__device__ void process_layer(const Params2D& P, const LayerStore& S, const int m, const LayerIO& in,
-                              const Batch2D& b, int* s_ws) {
+// Query order of a search phase: queries bucketed by their candidate count,
+// heaviest first, so that the lanes of a warp have similar trip counts.  The
+// order only decides which thread runs which query; results do not depend on it.
+template <int NT, class TT>
+__device__ void order_queries(const LayerStore<TT>& S, const int m, const float d, int* tmp, int* s_bins) {
+  constexpr int NB = 64;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < NB; i += NT) s_bins[i] = 0;
+  __syncthreads();
+  for (int q = tid; q < m; q += NT) {
+    const float2 p = S.xy[q];
+    const int bx0 = tile_bin(__fsub_rn(p.x, d)), bx1 = tile_bin(__fadd_rn(p.x, d));
+    const int by0 = tile_bin(__fsub_rn(p.y, d)), by1 = tile_bin(__fadd_rn(p.y, d));
+    int cnt = 0;
+    for (int c = bx0; c <= bx1; ++c) cnt += max(0, (int)S.tbl[c * kGridCols + by1 + 1] - (int)S.tbl[c * kGridCols + by0]);
+    const int bk = NB - 1 - min(cnt >> 2, NB - 1);
+    tmp[q] = bk;
+    atomicAdd(&s_bins[bk], 1);
+  }
+  __syncthreads();
+  if (tid < 32) {
+    const int a = s_bins[2 * tid], c = s_bins[2 * tid + 1];
+    int x = a + c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, x, o);
+      if (tid >= o) x += t;
+    }
+    const int ex = x - a - c;
+    s_bins[2 * tid] = ex;
+    s_bins[2 * tid + 1] = ex + a;
+  }
+  __syncthreads();
+  for (int q = tid; q < m; q += NT) S.qord[atomicAdd(&s_bins[tmp[q]], 1)] = q;
+  __syncthreads();
+}
+
+template <int NT, class TT>
+__device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const int m, const LayerIO& in,
+                              const Batch2D& b, int* s_ws, int* s_bins) {
   const int tid = threadIdx.x;
   int32_t* kkey = reinterpret_cast<int32_t*>(S.delta);  // sort key, later final slot
   int32_t* kprov = S.nh;                                 // provisional slot in tile
-  int32_t* slot_g = reinterpret_cast<int32_t*>(S.rho);  // gid at provisional slot
-  int32_t* slot_p = reinterpret_cast<int32_t*>(S.x);    // input position at provisional slot
+  int32_t* slot_g = S.qord;                              // gid at provisional slot
+  int32_t* slot_p = reinterpret_cast<int32_t*>(S.key);  // input position at provisional slot
 
   // -- counting sort into tiles (kernel_compute_histogram, CLUEAlgoKernels.h:18-23)
-  for (int i = tid; i < kTableInts; i += NT) S.tbl[i] = 0;
+  {
+    constexpr int kTableBytes = ((kTableInts * (int)sizeof(TT) + 15) / 16) * 16;
+    uint4* t4 = reinterpret_cast<uint4*>(S.tbl);
+    for (int i = tid; i < kTableBytes / 16; i += NT) t4[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
   __syncthreads();
   for (int p = tid; p < m; p += NT) {
     const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
     kkey[p] = key;
-    kprov[p] = atomicAdd(&S.tbl[key], 1);
+    kprov[p] = hist_add(S.tbl, key);
   }
   __syncthreads();
   block_scan_table<NT>(S.tbl, kTiles, s_ws);
   for (int p = tid; p < m; p += NT) {
-    const int q = S.tbl[kkey[p]] + kprov[p];
+    const int q = (int)S.tbl[kkey[p]] + kprov[p];
     slot_g[q] = in.gid ? in.gid[p] : in.gid_base + p;
     slot_p[q] = p;
   }
@@ -164,7 +241,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore& S, const int 
   for (int q = tid; q < m; q += NT) {
     const int p = slot_p[q];
     const int key = kkey[p];
-    const int s = S.tbl[key], e = S.tbl[key + 1];
+    const int s = (int)S.tbl[key], e = (int)S.tbl[key + 1];
     const int g = slot_g[q];
     int rank = 0;
     for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
@@ -174,58 +251,73 @@ __device__ void process_layer(const Params2D& P, const LayerStore& S, const int 
   for (int p = tid; p < m; p += NT) {
     const int f = kkey[p];
     const float wv = in.w[p];
-    S.x[f] = in.x[p];
-    S.y[f] = in.y[p];
-    S.w[f] = wv;
+    S.xy[f] = make_float2(in.x[p], in.y[p]);
     S.hw[f] = __fmul_rn(0.5f, wv);
-    S.gid[f] = in.gid ? in.gid[p] : in.gid_base + p;
+    S.nh[f] = __float_as_int(wv);
+    S.key[f] = (unsigned long long)(unsigned)(in.gid ? in.gid[p] : in.gid_base + p);
   }
   __syncthreads();
 
   // -- local density (kernel_calculate_density, CLUEAlgoKernels.h:25-55)
-  for (int q = tid; q < m; q += NT) {
-    const float xi = S.x[q], yi = S.y[q], wi = S.w[q];
-    const int bx0 = tile_bin(__fsub_rn(xi, P.dc)), bx1 = tile_bin(__fadd_rn(xi, P.dc));
-    const int by0 = tile_bin(__fsub_rn(yi, P.dc)), by1 = tile_bin(__fadd_rn(yi, P.dc));
+  order_queries<NT>(S, m, P.dc, kkey, s_bins);
+  for (int i = tid; i < m; i += NT) {
+    const int q = S.qord[i];
+    const float2 pq = S.xy[q];
+    const float wq = __int_as_float(S.nh[q]);
+    const int bx0 = tile_bin(__fsub_rn(pq.x, P.dc)), bx1 = tile_bin(__fadd_rn(pq.x, P.dc));
+    const int by0 = tile_bin(__fsub_rn(pq.y, P.dc)), by1 = tile_bin(__fadd_rn(pq.y, P.dc));
     float r = 0.f;
-    for (int c = bx0; c <= bx1; ++c) {
-      const int s = S.tbl[c * kGridCols + by0], e = S.tbl[c * kGridCols + by1 + 1];
-      for (int k = s; k < e; ++k) {
-        const float dx = __fsub_rn(xi, S.x[k]);
-        const float dy = __fsub_rn(yi, S.y[k]);
-        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-        if (d2 <= P.t_dc) r = __fadd_rn(r, (k == q) ? wi : S.hw[k]);
+    // candidates of all columns as one flattened sequence, in the reference order
+    int c = bx0 - 1, k = 0, e = 0;
+    for (;;) {
+      if (k >= e) {
+        if (++c > bx1) break;
+        k = (int)S.tbl[c * kGridCols + by0];
+        e = (int)S.tbl[c * kGridCols + by1 + 1];
+        continue;
       }
+      const float d2 = dist2(pq, S.xy[k]);
+      if (d2 <= P.t_dc) r = __fadd_rn(r, (k == q) ? wq : S.hw[k]);
+      ++k;
     }
-    S.rho[q] = r;
+    const unsigned g = (unsigned)S.key[q];
+    b.rho[in.ev_start + g] = r;
+    S.key[q] = ((unsigned long long)float_ord(r) << 32) | g;
   }
   __syncthreads();
 
   // -- distance to the nearest higher (kernel_calculate_distanceToHigher, :57-106)
-  for (int q = tid; q < m; q += NT) {
-    const float xi = S.x[q], yi = S.y[q], ri = S.rho[q];
-    const int gi = S.gid[q];
-    const int bx0 = tile_bin(__fsub_rn(xi, P.dm)), bx1 = tile_bin(__fadd_rn(xi, P.dm));
-    const int by0 = tile_bin(__fsub_rn(yi, P.dm)), by1 = tile_bin(__fadd_rn(yi, P.dm));
+  // "higher" (rho_j > rho_i, or equal rho and j > i) is key_j > key_i; a NaN
+  // rho is higher than nothing and nothing is higher than it, as in the reference.
+  order_queries<NT>(S, m, P.dm, reinterpret_cast<int32_t*>(S.delta), s_bins);
+  for (int i = tid; i < m; i += NT) {
+    const int q = S.qord[i];
+    const float2 pq = S.xy[q];
+    const unsigned long long ks = S.key[q];
+    const unsigned long long kq = (ks >> 32) == 0ull ? ~0ull : ks;
+    const int bx0 = tile_bin(__fsub_rn(pq.x, P.dm)), bx1 = tile_bin(__fadd_rn(pq.x, P.dm));
+    const int by0 = tile_bin(__fsub_rn(pq.y, P.dm)), by1 = tile_bin(__fadd_rn(pq.y, P.dm));
     float best_s = FLT_MAX, best_d2 = INFINITY;
     int best = -1;
-    for (int c = bx0; c <= bx1; ++c) {
-      const int s = S.tbl[c * kGridCols + by0], e = S.tbl[c * kGridCols + by1 + 1];
-      for (int k = s; k < e; ++k) {
-        const float rk = S.rho[k];
-        const bool higher = (rk > ri) || (rk == ri && S.gid[k] > gi);
-        const float dx = __fsub_rn(xi, S.x[k]);
-        const float dy = __fsub_rn(yi, S.y[k]);
-        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-        if (higher && d2 <= P.t_dm && d2 < best_d2) {
-          const float sd = __fsqrt_rn(d2);
-          if (sd < best_s) {
-            best_s = sd;
-            best_d2 = d2;
-            best = k;
-          }
+    int c = bx0 - 1, k = 0, e = 0;
+    for (;;) {
+      if (k >= e) {
+        if (++c > bx1) break;
+        k = (int)S.tbl[c * kGridCols + by0];
+        e = (int)S.tbl[c * kGridCols + by1 + 1];
+        continue;
+      }
+      const unsigned long long kk = S.key[k];
+      const float d2 = dist2(pq, S.xy[k]);
+      if (kk > kq && d2 <= P.t_dm && d2 < best_d2) {
+        const float sd = __fsqrt_rn(d2);
+        if (sd < best_s) {
+          best_s = sd;
+          best_d2 = d2;
+          best = k;
         }
       }
+      ++k;
     }
     S.delta[q] = best_s;
     S.nh[q] = best;
@@ -235,14 +327,15 @@ __device__ void process_layer(const Params2D& P, const LayerStore& S, const int 
   // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
   int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
   for (int q = tid; q < m; q += NT) {
-    const float r = S.rho[q], d = S.delta[q];
+    const unsigned long long ks = S.key[q];
+    const float r = ord_float((unsigned)(ks >> 32));
+    const float d = S.delta[q];
     const int n = S.nh[q];
     const bool seed = (d > P.dc) && (r >= P.rhoc);
     const bool outlier = (d > P.dm) && (r < P.rhoc);
-    const int64_t o = in.ev_start + S.gid[q];
-    b.rho[o] = r;
+    const int64_t o = in.ev_start + (unsigned)ks;
     b.delta[o] = d;
-    b.nh[o] = n >= 0 ? S.gid[n] : -1;
+    b.nh[o] = n >= 0 ? (int)(unsigned)S.key[n] : -1;
     b.seed[o] = seed ? 1 : 0;
     par[q] = (!seed && !outlier && n >= 0) ? n : (seed ? -2 : -3);
   }
@@ -266,11 +359,10 @@ __device__ void process_layer(const Params2D& P, const LayerStore& S, const int 
     const int p = par[q];
     const int root = p >= 0 ? p : q;
     // seed roots carry their event-local index until k_seed_rank/k_label
-    b.ci[in.ev_start + S.gid[q]] = (par[root] == -2) ? S.gid[root] : -1;
+    b.ci[in.ev_start + (unsigned)S.key[q]] = (par[root] == -2) ? (int)(unsigned)S.key[root] : -1;
   }
   __syncthreads();
 }
-
 // ------------------------------------------------------------------ kernels
 
 __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
@@ -370,20 +462,19 @@ __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ int s_item;
   __shared__ int s_ws[33];
+  __shared__ int s_bins[64];
   const int n_items = b.n_events * kLayers;
   const bool grouped = b.flags[kFlagGrouped] != 0;
-  LayerStore sm;
-  sm.tbl = reinterpret_cast<int32_t*>(dsm);
+  LayerStore<uint16_t> sm;
+  sm.tbl = reinterpret_cast<uint16_t*>(dsm);
   {
-    unsigned char* p = dsm + ((kTableInts * 4 + 15) / 16) * 16;
-    sm.x = reinterpret_cast<float*>(p);
-    sm.y = sm.x + cap;
-    sm.hw = sm.y + cap;
-    sm.w = sm.hw + cap;
-    sm.gid = reinterpret_cast<int32_t*>(sm.w + cap);
-    sm.rho = reinterpret_cast<float*>(sm.gid + cap);
-    sm.delta = sm.rho + cap;
+    unsigned char* p = dsm + ((kTableInts * 2 + 15) / 16) * 16;
+    sm.xy = reinterpret_cast<float2*>(p);
+    sm.key = reinterpret_cast<unsigned long long*>(sm.xy + cap);
+    sm.hw = reinterpret_cast<float*>(sm.key + cap);
+    sm.delta = sm.hw + cap;
     sm.nh = reinterpret_cast<int32_t*>(sm.delta + cap);
+    sm.qord = sm.nh + cap;
   }
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(&b.flags[kFlagTicket], 1);
@@ -412,24 +503,22 @@ __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
       io.gid_base = 0;
     }
     if (m <= cap) {
-      process_layer<NT>(P, sm, m, io, b, s_ws);
+      process_layer<NT>(P, sm, m, io, b, s_ws, s_bins);
     } else {
-      LayerStore g;
-      g.x = b.sp[0] + start;
-      g.y = b.sp[1] + start;
-      g.hw = b.sp[2] + start;
-      g.w = b.sp[3] + start;
-      g.gid = reinterpret_cast<int32_t*>(b.sp[4]) + start;
-      g.rho = b.sp[5] + start;
-      g.delta = b.sp[6] + start;
-      g.nh = reinterpret_cast<int32_t*>(b.sp[7]) + start;
-      g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableInts;
+      // spill: the same stages on HBM scratch at this layer's grouped position
+      LayerStore<int32_t> g;
+      g.xy = reinterpret_cast<float2*>(b.sp[0]) + start;
+      g.key = reinterpret_cast<unsigned long long*>(b.sp[2]) + start;
+      g.hw = b.sp[4] + start;
+      g.delta = b.sp[5] + start;
+      g.nh = reinterpret_cast<int32_t*>(b.sp[6]) + start;
+      g.qord = reinterpret_cast<int32_t*>(b.sp[7]) + start;
+      g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableStride;
       if (threadIdx.x == 0) atomicAdd(&b.flags[kFlagSpilled], 1);
-      process_layer<NT>(P, g, m, io, b, s_ws);
+      process_layer<NT>(P, g, m, io, b, s_ws, s_bins);
     }
   }
 }
-
 // Seeds per event-aligned chunk.
 __global__ void __launch_bounds__(kChunkThreads) k_seed_count(Batch2D b) {
   const int c = blockIdx.x;
@@ -578,7 +667,8 @@ Params2D make_params2d(float dc, float rhoc, float odf) {
 }
 
 size_t layer_smem_bytes(const Tuning2D& t) {
-  return ((size_t)(kTableInts * 4 + 15) / 16) * 16 + (size_t)t.layer_capacity * 32;
+  // 16-bit tile table, then 32 bytes per point (see LayerStore)
+  return ((size_t)(kTableInts * 2 + 15) / 16) * 16 + (size_t)t.layer_capacity * 32;
 }
 
 int layer_grid(const Tuning2D& t, int n_items) {

@@ -14,6 +14,8 @@ constexpr int kLayers = 100;
 constexpr int kGridCols = 100;
 constexpr int kTiles = kGridCols * kGridCols;
 constexpr int kTableInts = kTiles + 1;
+// Per-CTA stride of the HBM tile tables (32-bit counts), a multiple of 16 bytes.
+constexpr int kTableStride = ((kTableInts * 4 + 15) / 16) * 4;
 // Points per event-aligned chunk of the streaming kernels (count, scatter, seed ranks).
 constexpr int kChunk = 4096;
 constexpr int kChunkThreads = 512;

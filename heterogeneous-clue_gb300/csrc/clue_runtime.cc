@@ -119,8 +119,11 @@ std::vector<size_t> sizes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bo
   s[S_CS] = 4 * (size_t)(E + 1);
   s[S_LCNT] = s[S_LSTART] = s[S_CURSOR] = 4 * (size_t)E * kLayers;
   s[S_GX] = s[S_GY] = s[S_GW] = s[S_GID] = 4 * (size_t)N;
-  for (int i = S_SP0; i <= S_SP7; ++i) s[i] = 4 * (size_t)N;
-  s[S_SPTBL] = 4 * (size_t)kTableInts * grid;
+  // spill homes: xy (8 B), key (8 B), then hw, delta, nh, qord (4 B each)
+  s[S_SP0] = s[S_SP2] = 8 * (size_t)N;
+  s[S_SP1] = s[S_SP3] = 0;
+  s[S_SP4] = s[S_SP5] = s[S_SP6] = s[S_SP7] = 4 * (size_t)N;
+  s[S_SPTBL] = 4 * (size_t)kTableStride * grid;
   s[S_CSEED] = s[S_CBASE] = 4 * (size_t)std::max<int64_t>(nchunks, 1);
   s[S_FLAGS] = 4 * kFlagCount;
   if (host_io) {
@@ -346,7 +349,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
   h->error_layers = kLayers;
-  if (host_io) {
+  if (host_io && !(r.flags & kAsyncHostIO)) {
     rc = h->wait_previous();
     if (rc) return rc;
     return h->check_device_flags();

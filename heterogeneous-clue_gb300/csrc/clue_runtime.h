@@ -62,6 +62,10 @@ struct GraphKey {
 
 size_t required_bytes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bool host_io);
 
+// Internal run flag: host (pinned) buffers, but return once the work is
+// queued; completion is seen through Handle::done_event.  Used by the server.
+constexpr int kAsyncHostIO = 0x100;
+
 struct Handle {
   int device = 0;
   size_t budget = 0;

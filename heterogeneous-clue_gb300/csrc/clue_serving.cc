@@ -1,0 +1,398 @@
+// Serving loop: continuous batching of CLUE 2D events (no reference
+// counterpart; the reference runs a fixed set of events per EDM stream,
+// src/serial/bin/StreamSchedule.cc:61-93).
+//
+// Requests are queued by clue_server_submit (inputs copied on submit).  A
+// scheduler thread owns `max_inflight` slots; each slot is a CLUE handle with
+// its own CUDA stream, resident device buffers and pinned staging, sized to
+// an equal share of the device-memory budget.  Whenever a slot is free and
+// requests are waiting, the scheduler admits as many queued events as fit
+// the slot (points and event count), stages them, and launches the batched
+// pipeline asynchronously; batches of different slots overlap on the device
+// (one batch's copies with another's kernels).  Completed batches are found
+// with cudaEventQuery, their outputs are copied to each caller's buffers,
+// and the request latency (submit -> outputs written) is recorded.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/clue.h"
+#include "clue_internal.h"
+#include "clue_runtime.h"
+
+namespace clue {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  int64_t id = 0;
+  int32_t n = 0;
+  std::vector<float> x, y, w;
+  std::vector<int32_t> layer;
+  clue_outputs out{};
+  Clock::time_point t_submit;
+  double latency_ms = 0.0;
+  int status = CLUE_EBUSY;
+};
+
+struct Slot {
+  clue_handle* h = nullptr;
+  PinnedBuf in, out;
+  std::vector<int64_t> off;
+  std::vector<Request*> reqs;
+  bool busy = false;
+  int64_t cap_points = 0;
+};
+
+class Server {
+ public:
+  Server(const clue_params& p, const clue_server_config& c) : params_(p), cfg_(c) {}
+  ~Server() { shutdown(); }
+
+  int start() {
+    if (cfg_.max_inflight < 1) cfg_.max_inflight = 1;
+    if (cfg_.max_batch_events < 1) cfg_.max_batch_events = 1;
+    if (!cfg_.device_budget_bytes) cfg_.device_budget_bytes = size_t(16) << 30;
+    const size_t share = cfg_.device_budget_bytes / cfg_.max_inflight;
+    slots_.resize(cfg_.max_inflight);
+    for (auto& s : slots_) {
+      int rc = clue_create(&params_, share, cfg_.device, nullptr, &s.h);
+      if (rc) return rc;
+      Handle* hh = reinterpret_cast<Handle*>(s.h);
+      // largest point count whose batch fits this slot's share
+      int64_t lo = 0, hi = int64_t(1) << 31;
+      const int grid = layer_grid(hh->tuning, cfg_.max_batch_events * kLayers);
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) / 2;
+        const int64_t chunks = mid / kChunk + cfg_.max_batch_events;
+        if (required_bytes_2d(cfg_.max_batch_events, mid, chunks, grid, true) <= share) lo = mid; else hi = mid;
+      }
+      s.cap_points = lo;
+      if (s.cap_points < 1) return set_error(CLUE_ENOMEM, "budget too small for one in-flight batch");
+    }
+    cap_points_ = slots_[0].cap_points;
+    worker_ = std::thread([this] { loop(); });
+    return CLUE_OK;
+  }
+
+  void shutdown() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      if (stop_) return;
+      stop_ = true;
+    }
+    cv_.notify_all();
+    if (worker_.joinable()) worker_.join();
+    for (auto& s : slots_) {
+      if (s.h) clue_destroy(s.h);
+      s.h = nullptr;
+    }
+    for (auto& kv : reqs_) delete kv.second;
+    reqs_.clear();
+  }
+
+  int submit(int32_t n, const float* x, const float* y, const int32_t* layer, const float* w,
+             const clue_outputs* out, int64_t* id) {
+    if (n < 0 || !out || !id || (n > 0 && (!x || !y || !layer || !w))) return set_error(CLUE_EINVAL, "bad argument");
+    if (n > cap_points_)
+      return set_error(CLUE_ENOMEM, "event of %d points exceeds one in-flight batch (%lld points)", n,
+                       (long long)cap_points_);
+    Request* r = new Request();
+    r->n = n;
+    r->x.assign(x, x + n);
+    r->y.assign(y, y + n);
+    r->w.assign(w, w + n);
+    r->layer.assign(layer, layer + n);
+    r->out = *out;
+    r->t_submit = Clock::now();
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      r->id = next_id_++;
+      reqs_[r->id] = r;
+      queue_.push_back(r);
+      *id = r->id;
+    }
+    cv_.notify_all();
+    return CLUE_OK;
+  }
+
+  int poll(int64_t id, int32_t timeout_ms, double* lat) {
+    std::unique_lock<std::mutex> g(mu_);
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) return set_error(CLUE_EINVAL, "unknown request id %lld", (long long)id);
+    Request* r = it->second;
+    auto ready = [&] { return r->status != CLUE_EBUSY; };
+    if (!ready()) {
+      if (timeout_ms == 0) return CLUE_EBUSY;
+      if (timeout_ms < 0) {
+        done_cv_.wait(g, ready);
+      } else if (!done_cv_.wait_for(g, std::chrono::milliseconds(timeout_ms), ready)) {
+        return set_error(CLUE_ETIMEOUT, "request %lld not finished after %d ms", (long long)id, timeout_ms);
+      }
+    }
+    const int st = r->status;
+    if (lat) *lat = r->latency_ms;
+    reqs_.erase(it);
+    delete r;
+    if (st != CLUE_OK) return set_error(st, "request %lld failed", (long long)id);
+    return CLUE_OK;
+  }
+
+  int drain(int32_t timeout_ms) {
+    std::unique_lock<std::mutex> g(mu_);
+    auto idle = [&] {
+      if (!queue_.empty()) return false;
+      for (auto& s : slots_)
+        if (s.busy) return false;
+      return true;
+    };
+    if (timeout_ms < 0) {
+      done_cv_.wait(g, idle);
+    } else if (!done_cv_.wait_for(g, std::chrono::milliseconds(timeout_ms), idle)) {
+      return set_error(CLUE_ETIMEOUT, "server not drained after %d ms", timeout_ms);
+    }
+    return CLUE_OK;
+  }
+
+  void stats(clue_server_stats* st) {
+    std::lock_guard<std::mutex> g(mu_);
+    st->completed = (int64_t)lat_.size();
+    st->batches = batches_;
+    std::vector<double> v = lat_;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) {
+      if (v.empty()) return 0.0;
+      size_t i = (size_t)std::min<double>(v.size() - 1, std::max(0.0, q * v.size() - 1e-9));
+      return v[i];
+    };
+    st->p50_ms = pct(0.50);
+    st->p99_ms = pct(0.99);
+    st->mean_batch_events = batches_ ? double(batched_events_) / batches_ : 0.0;
+    st->max_inflight_seen = max_inflight_seen_;
+  }
+
+  void reset_stats() {
+    std::lock_guard<std::mutex> g(mu_);
+    lat_.clear();
+    batches_ = 0;
+    batched_events_ = 0;
+    max_inflight_seen_ = 0;
+  }
+
+ private:
+  // Completes every finished slot; called with mu_ held.
+  bool reap() {
+    bool any = false;
+    for (auto& s : slots_) {
+      if (!s.busy) continue;
+      Handle* h = reinterpret_cast<Handle*>(s.h);
+      cudaError_t q = cudaEventQuery(h->done_event);
+      if (q == cudaErrorNotReady) continue;
+      int st = CLUE_OK;
+      if (q != cudaSuccess) {
+        st = cuda_error(q, "serving batch");
+      } else {
+        h->pending = false;
+        st = h->check_device_flags();
+      }
+      const auto now = Clock::now();
+      const char* ob = static_cast<const char*>(s.out.p);
+      const int64_t N = s.off.back();
+      for (size_t k = 0; k < s.reqs.size(); ++k) {
+        Request* r = s.reqs[k];
+        const int64_t o = s.off[k];
+        const size_t b = 4 * (size_t)r->n;
+        if (st == CLUE_OK && r->n > 0) {
+          memcpy(r->out.rho, ob + 4 * o, b);
+          memcpy(r->out.delta, ob + 4 * (N + o), b);
+          memcpy(r->out.nearestHigher, ob + 4 * (2 * N + o), b);
+          memcpy(r->out.isSeed, ob + 4 * (3 * N + o), b);
+          memcpy(r->out.clusterIndex, ob + 4 * (4 * N + o), b);
+        }
+        r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
+        r->status = st;
+        if (st == CLUE_OK) lat_.push_back(r->latency_ms);
+        r->x.clear();
+        r->x.shrink_to_fit();
+        r->y.clear();
+        r->y.shrink_to_fit();
+        r->w.clear();
+        r->w.shrink_to_fit();
+        r->layer.clear();
+        r->layer.shrink_to_fit();
+      }
+      s.reqs.clear();
+      s.busy = false;
+      any = true;
+    }
+    if (any) done_cv_.notify_all();
+    return any;
+  }
+
+  // Admits queued requests into a free slot and launches it; mu_ held.
+  void admit(Slot& s) {
+    s.reqs.clear();
+    s.off.assign(1, 0);
+    int64_t pts = 0;
+    while (!queue_.empty() && (int)s.reqs.size() < cfg_.max_batch_events) {
+      Request* r = queue_.front();
+      if (pts + r->n > s.cap_points && !s.reqs.empty()) break;
+      queue_.pop_front();
+      s.reqs.push_back(r);
+      pts += r->n;
+      s.off.push_back(pts);
+    }
+    const int32_t E = (int32_t)s.reqs.size();
+    if (E == 0) return;
+    int rc = s.in.reserve(16 * (size_t)std::max<int64_t>(pts, 1));
+    if (!rc) rc = s.out.reserve(20 * (size_t)std::max<int64_t>(pts, 1));
+    if (!rc) {
+      char* ib = static_cast<char*>(s.in.p);
+      for (int32_t k = 0; k < E; ++k) {
+        Request* r = s.reqs[k];
+        const int64_t o = s.off[k];
+        const size_t b = 4 * (size_t)r->n;
+        memcpy(ib + 4 * o, r->x.data(), b);
+        memcpy(ib + 4 * (pts + o), r->y.data(), b);
+        memcpy(ib + 4 * (2 * pts + o), r->layer.data(), b);
+        memcpy(ib + 4 * (3 * pts + o), r->w.data(), b);
+      }
+      char* ob = static_cast<char*>(s.out.p);
+      clue_outputs out{reinterpret_cast<float*>(ob), reinterpret_cast<float*>(ob + 4 * pts),
+                       reinterpret_cast<int32_t*>(ob + 8 * pts), reinterpret_cast<int32_t*>(ob + 12 * pts),
+                       reinterpret_cast<int32_t*>(ob + 16 * pts)};
+      Handle* h = reinterpret_cast<Handle*>(s.h);
+      rc = h->run_batch(E, s.off.data(), reinterpret_cast<const float*>(ib),
+                        reinterpret_cast<const float*>(ib + 4 * pts),
+                        reinterpret_cast<const int32_t*>(ib + 8 * pts),
+                        reinterpret_cast<const float*>(ib + 12 * pts), &out,
+                        CLUE_HOST_MEMORY | CLUE_NO_GRAPH | kAsyncHostIO);
+    }
+    if (rc) {
+      for (Request* r : s.reqs) {
+        r->status = rc;
+        r->latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
+      }
+      s.reqs.clear();
+      done_cv_.notify_all();
+      return;
+    }
+    s.busy = true;
+    ++batches_;
+    batched_events_ += E;
+    int inflight = 0;
+    for (auto& t : slots_) inflight += t.busy;
+    max_inflight_seen_ = std::max<double>(max_inflight_seen_, inflight);
+  }
+
+  void loop() {
+    cudaSetDevice(cfg_.device);
+    std::unique_lock<std::mutex> g(mu_);
+    while (!stop_) {
+      reap();
+      Slot* free_slot = nullptr;
+      bool busy = false;
+      for (auto& s : slots_) {
+        if (!s.busy && !free_slot) free_slot = &s;
+        busy |= s.busy;
+      }
+      if (free_slot && !queue_.empty()) {
+        admit(*free_slot);
+        continue;
+      }
+      if (busy) {
+        // batches in flight: look again shortly (new arrivals wake us earlier)
+        cv_.wait_for(g, std::chrono::microseconds(50));
+      } else {
+        cv_.wait_for(g, std::chrono::milliseconds(5));
+      }
+    }
+    // finish what is in flight before the slots are destroyed
+    for (auto& s : slots_)
+      if (s.busy) cudaEventSynchronize(reinterpret_cast<Handle*>(s.h)->done_event);
+    reap();
+    for (Request* r : queue_) r->status = CLUE_EINVAL;
+    queue_.clear();
+    done_cv_.notify_all();
+  }
+
+  clue_params params_;
+  clue_server_config cfg_;
+  std::vector<Slot> slots_;
+  int64_t cap_points_ = 0;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  std::deque<Request*> queue_;
+  std::unordered_map<int64_t, Request*> reqs_;
+  int64_t next_id_ = 1;
+  bool stop_ = false;
+  std::thread worker_;
+  std::vector<double> lat_;
+  int64_t batches_ = 0, batched_events_ = 0;
+  double max_inflight_seen_ = 0;
+};
+
+}  // namespace
+}  // namespace clue
+
+using clue::Server;
+using clue::set_error;
+
+extern "C" {
+
+int clue_server_create(const clue_params* params, const clue_server_config* cfg, clue_server** out) {
+  if (!params || !cfg || !out) return set_error(CLUE_EINVAL, "NULL argument");
+  *out = nullptr;
+  Server* s = new Server(*params, *cfg);
+  int rc = s->start();
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  *out = reinterpret_cast<clue_server*>(s);
+  return CLUE_OK;
+}
+
+int clue_server_destroy(clue_server* s) {
+  delete reinterpret_cast<Server*>(s);
+  return CLUE_OK;
+}
+
+int clue_server_submit(clue_server* s, int32_t n, const float* x, const float* y, const int32_t* layer,
+                       const float* weight, const clue_outputs* out, int64_t* request_id) {
+  if (!s) return set_error(CLUE_EINVAL, "NULL server");
+  return reinterpret_cast<Server*>(s)->submit(n, x, y, layer, weight, out, request_id);
+}
+
+int clue_server_poll(clue_server* s, int64_t id, int32_t timeout_ms, double* latency_ms) {
+  if (!s) return set_error(CLUE_EINVAL, "NULL server");
+  return reinterpret_cast<Server*>(s)->poll(id, timeout_ms, latency_ms);
+}
+
+int clue_server_drain(clue_server* s, int32_t timeout_ms) {
+  if (!s) return set_error(CLUE_EINVAL, "NULL server");
+  return reinterpret_cast<Server*>(s)->drain(timeout_ms);
+}
+
+int clue_server_get_stats(clue_server* s, clue_server_stats* st) {
+  if (!s || !st) return set_error(CLUE_EINVAL, "NULL argument");
+  reinterpret_cast<Server*>(s)->stats(st);
+  return CLUE_OK;
+}
+
+int clue_server_reset_stats(clue_server* s) {
+  if (!s) return set_error(CLUE_EINVAL, "NULL server");
+  reinterpret_cast<Server*>(s)->reset_stats();
+  return CLUE_OK;
+}
+
+}  // extern "C"

@@ -139,7 +139,7 @@ def test_spill_path_matches(algo):
     assert_bitexact(got, oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *PRM))
 
 
-@pytest.mark.parametrize("threads,cap", [(256, 1024), (512, 3072), (1024, 4096), (512, 5632)])
+@pytest.mark.parametrize("threads,cap", [(256, 1024), (512, 3072), (1024, 4096), (512, 6144), (256, 2048)])
 def test_tunings_give_identical_results(algo, threads, cap):
     b = S.uneven_batch(6, seed=15, lo=5000, hi=200000)
     t = algo.get_tuning()

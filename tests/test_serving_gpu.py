@@ -1,0 +1,97 @@
+"""The serving loop: continuous batching with overlapping in-flight batches.
+
+The key property: every request's result is bit-identical whether the event
+runs alone (clue_run_event) or inside whatever batch the server formed."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import clue_gb300 as C
+import oracle
+from clue_gb300 import synthetic as S
+
+from _util import assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+PRM = (1.3, 2.0, 2.0)
+
+
+@pytest.fixture(scope="module")
+def events():
+    b = S.uneven_batch(48, seed=21, lo=2000, hi=120000)
+    return [S.event_of(b, e) for e in range(48)]
+
+
+@pytest.fixture(scope="module")
+def alone(events, cuda_lib):
+    a = C.Clusterizer(*PRM)
+    outs = [a.make_clusters(e["x"], e["y"], e["layer"], e["weight"]) for e in events]
+    a.close()
+    return outs
+
+
+def test_results_identical_alone_and_in_the_mix(events, alone):
+    srv = C.Server(*PRM, budget_bytes=8 << 30, max_inflight=2, max_batch_events=6)
+    rng = np.random.default_rng(3)
+    ids = [None] * len(events)
+    outs = [None] * len(events)
+
+    def client(k0):
+        for k in range(k0, len(events), 3):
+            time.sleep(float(rng.exponential(0.002)))
+            ids[k], outs[k] = srv.submit(**events[k])
+
+    th = [threading.Thread(target=client, args=(i,)) for i in range(3)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    lats = []
+    for k, rid in enumerate(ids):
+        st, lat = srv.poll(rid, timeout_ms=60000)
+        assert st == C.CLUE_OK
+        lats.append(lat)
+        assert_bitexact(outs[k], alone[k], label=f"request {k}")
+    stats = srv.stats()
+    assert stats["completed"] == len(events)
+    assert stats["batches"] < len(events), "no batching happened"
+    assert all(l > 0 for l in lats)
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
+    srv.close()
+
+
+def test_burst_overlaps_batches_on_device(events, alone):
+    srv = C.Server(*PRM, budget_bytes=8 << 30, max_inflight=2, max_batch_events=4)
+    reqs = [srv.submit(**e) for e in events]
+    srv.drain(timeout_ms=60000)
+    for k, (rid, out) in enumerate(reqs):
+        st, _ = srv.poll(rid, timeout_ms=0)
+        assert st == C.CLUE_OK
+        assert_bitexact(out, alone[k])
+    st = srv.stats()
+    assert st["max_inflight_seen"] >= 2, st
+    assert st["mean_batch_events"] > 1
+    srv.close()
+
+
+def test_one_request_against_the_oracle(events):
+    srv = C.Server(*PRM, budget_bytes=4 << 30, max_inflight=1, max_batch_events=8)
+    e = events[5]
+    rid, out = srv.submit(**e)
+    assert srv.poll(rid, timeout_ms=60000)[0] == C.CLUE_OK
+    assert_bitexact(out, oracle.clue2d(e["x"], e["y"], e["layer"], e["weight"], *PRM))
+    srv.close()
+
+
+def test_admission_rejects_an_event_larger_than_a_slot(events):
+    srv = C.Server(*PRM, budget_bytes=64 << 20, max_inflight=2, max_batch_events=4)
+    big = S.hgcal_event(1000)
+    with pytest.raises(C.ClueError) as ei:
+        srv.submit(**big)
+    assert ei.value.code == C.CLUE_ENOMEM
+    rid, out = srv.submit(**events[0])  # a small one still fits
+    assert srv.poll(rid, timeout_ms=60000)[0] == C.CLUE_OK
+    srv.close()
