@@ -91,23 +91,57 @@ __device__ __forceinline__ int block_inclusive_scan(int v, int* s_ws, int* total
   return res;
 }
 
-// Exclusive scan of tbl[0..n) in place, tbl[n] = total (tbl of 16- or 32-bit counts).
-template <int NT, class TT>
-__device__ void block_scan_table(TT* tbl, int n, int* s_ws) {
+// Exclusive scan of tbl[0..n) in place, tbl[n] = total (32-bit counts, HBM tables).
+template <int NT>
+__device__ void block_scan_table(int32_t* tbl, int n, int* s_ws) {
   const int per = (n + NT - 1) / NT;
   const int beg = min((int)threadIdx.x * per, n);
   const int end = min(beg + per, n);
   int sum = 0;
-  for (int i = beg; i < end; ++i) sum += (int)tbl[i];
+  for (int i = beg; i < end; ++i) sum += tbl[i];
   int total;
   const int incl = block_inclusive_scan<NT>(sum, s_ws, &total);
   int run = incl - sum;
   for (int i = beg; i < end; ++i) {
-    const int c = (int)tbl[i];
-    tbl[i] = (TT)run;
+    const int c = tbl[i];
+    tbl[i] = run;
     run += c;
   }
-  if (threadIdx.x == 0) tbl[n] = (TT)total;
+  if (threadIdx.x == 0) tbl[n] = total;
+  __syncthreads();
+}
+
+// The same for the on-chip 16-bit table: each thread scans whole 16-byte
+// groups of 8 counts (kTiles = 10000 is a multiple of 8).
+template <int NT>
+__device__ void block_scan_table(uint16_t* tbl, int n, int* s_ws) {
+  const int groups = n / 8;
+  const int per = (groups + NT - 1) / NT;
+  const int beg = min((int)threadIdx.x * per, groups);
+  const int end = min(beg + per, groups);
+  uint4* t4 = reinterpret_cast<uint4*>(tbl);
+  int sum = 0;
+  for (int g = beg; g < end; ++g) {
+    const uint4 v = t4[g];
+    const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sum += (int)(w[j] & 0xffffu) + (int)(w[j] >> 16);
+  }
+  int total;
+  const int incl = block_inclusive_scan<NT>(sum, s_ws, &total);
+  unsigned run = (unsigned)(incl - sum);
+  for (int g = beg; g < end; ++g) {
+    const uint4 v = t4[g];
+    unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const unsigned lo = w[j] & 0xffffu, hi = w[j] >> 16;
+      w[j] = run | ((run + lo) << 16);
+      run += lo + hi;
+    }
+    t4[g] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  if (threadIdx.x == 0) tbl[n] = (uint16_t)total;
   __syncthreads();
 }
 
@@ -149,15 +183,15 @@ __device__ __forceinline__ float ord_float(unsigned o) {
 }
 
 // Per-layer working set, sorted by tile: on-chip for layers up to the tuned
-// capacity, in HBM scratch beyond it.  32 bytes per point plus the table.
-template <class TT>
+// capacity (16-bit table and query order), in HBM scratch beyond it (32-bit).
+// 26 bytes per point on chip plus the 20 KB table.
+template <class TT, class QT>
 struct LayerStore {
   float2* xy;               // position
-  unsigned long long* key;  // (float_ord(rho) << 32) | gid; gid alone before rho exists
+  unsigned long long* key;  // (float_ord(rho) << 32) | gid; gid (+ a bucket above it) before rho exists
   float* hw;                // 0.5f * w, the reference's neighbour term
-  float* delta;
-  int32_t* nh;              // own weight (bits) during density, then nearest higher, then parent
-  int32_t* qord;            // query order of the current phase
+  int32_t* nh;              // own weight (bits) during density, then the parent pointer
+  QT* qord;                 // query order of the current search
   TT* tbl;                  // kTableInts: exclusive scan over key = xBin*100 + yBin
 };
 
@@ -170,11 +204,24 @@ struct LayerIO {
   int64_t ev_start;
 };
 
+__device__ __forceinline__ int candidate_count(const uint16_t* tbl, int bx0, int bx1, int by0, int by1) {
+  int cnt = 0;
+  for (int c = bx0; c <= bx1; ++c) cnt += max(0, (int)tbl[c * kGridCols + by1 + 1] - (int)tbl[c * kGridCols + by0]);
+  return cnt;
+}
+__device__ __forceinline__ int candidate_count(const int32_t* tbl, int bx0, int bx1, int by0, int by1) {
+  int cnt = 0;
+  for (int c = bx0; c <= bx1; ++c) cnt += max(0, tbl[c * kGridCols + by1 + 1] - tbl[c * kGridCols + by0]);
+  return cnt;
+}
+
 // Query order of a search phase: queries bucketed by their candidate count,
-// heaviest first, so that the lanes of a warp have similar trip counts.  The
-// order only decides which thread runs which query; results do not depend on it.
-template <int NT, class TT>
-__device__ void order_queries(const LayerStore<TT>& S, const int m, const float d, int* tmp, int* s_bins) {
+// heaviest first; warps then take chunks of 32 in that order.  Which thread
+// runs which query never changes a result.  `bucket_of(q)` / `set_bucket`
+// park the bucket in a word the phase does not need yet.
+template <int NT, class TT, class QT, class Get, class Set>
+__device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const float d, int* s_bins, Get bucket_of,
+                              Set set_bucket) {
   constexpr int NB = 64;
   const int tid = threadIdx.x;
   for (int i = tid; i < NB; i += NT) s_bins[i] = 0;
@@ -183,10 +230,9 @@ __device__ void order_queries(const LayerStore<TT>& S, const int m, const float 
     const float2 p = S.xy[q];
     const int bx0 = tile_bin(__fsub_rn(p.x, d)), bx1 = tile_bin(__fadd_rn(p.x, d));
     const int by0 = tile_bin(__fsub_rn(p.y, d)), by1 = tile_bin(__fadd_rn(p.y, d));
-    int cnt = 0;
-    for (int c = bx0; c <= bx1; ++c) cnt += max(0, (int)S.tbl[c * kGridCols + by1 + 1] - (int)S.tbl[c * kGridCols + by0]);
+    const int cnt = candidate_count(S.tbl, bx0, bx1, by0, by1);
     const int bk = NB - 1 - min(cnt >> 2, NB - 1);
-    tmp[q] = bk;
+    set_bucket(q, bk);
     atomicAdd(&s_bins[bk], 1);
   }
   __syncthreads();
@@ -203,18 +249,25 @@ __device__ void order_queries(const LayerStore<TT>& S, const int m, const float 
     s_bins[2 * tid + 1] = ex + a;
   }
   __syncthreads();
-  for (int q = tid; q < m; q += NT) S.qord[atomicAdd(&s_bins[tmp[q]], 1)] = q;
+  for (int q = tid; q < m; q += NT) S.qord[atomicAdd(&s_bins[bucket_of(q)], 1)] = (QT)q;
   __syncthreads();
 }
 
-template <int NT, class TT>
-__device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const int m, const LayerIO& in,
-                              const Batch2D& b, int* s_ws, int* s_bins) {
-  const int tid = threadIdx.x;
-  int32_t* kkey = reinterpret_cast<int32_t*>(S.delta);  // sort key, later final slot
+// Next chunk of 32 queries for this warp (dynamic, in query order).
+__device__ __forceinline__ int next_chunk(int* s_next) {
+  int base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(s_next, 32);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
+template <int NT, class TT, class QT>
+__device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, const int m, const LayerIO& in,
+                              const Batch2D& b, int* s_ws, int* s_bins, int* s_next) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  QT* kkey = S.qord;                                     // sort key, later final slot
   int32_t* kprov = S.nh;                                 // provisional slot in tile
-  int32_t* slot_g = S.qord;                              // gid at provisional slot
   int32_t* slot_p = reinterpret_cast<int32_t*>(S.key);  // input position at provisional slot
+  int32_t* slot_g = slot_p + m;                          // gid at provisional slot
 
   // -- counting sort into tiles (kernel_compute_histogram, CLUEAlgoKernels.h:18-23)
   {
@@ -225,7 +278,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const 
   __syncthreads();
   for (int p = tid; p < m; p += NT) {
     const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
-    kkey[p] = key;
+    kkey[p] = (QT)key;
     kprov[p] = hist_add(S.tbl, key);
   }
   __syncthreads();
@@ -240,16 +293,16 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const 
   // index order, so place each point at its gid rank within the tile.
   for (int q = tid; q < m; q += NT) {
     const int p = slot_p[q];
-    const int key = kkey[p];
+    const int key = (int)kkey[p];
     const int s = (int)S.tbl[key], e = (int)S.tbl[key + 1];
     const int g = slot_g[q];
     int rank = 0;
     for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
-    kkey[p] = s + rank;
+    kkey[p] = (QT)(s + rank);
   }
   __syncthreads();
   for (int p = tid; p < m; p += NT) {
-    const int f = kkey[p];
+    const int f = (int)kkey[p];
     const float wv = in.w[p];
     S.xy[f] = make_float2(in.x[p], in.y[p]);
     S.hw[f] = __fmul_rn(0.5f, wv);
@@ -259,39 +312,70 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const 
   __syncthreads();
 
   // -- local density (kernel_calculate_density, CLUEAlgoKernels.h:25-55)
-  order_queries<NT>(S, m, P.dc, kkey, s_bins);
-  for (int i = tid; i < m; i += NT) {
-    const int q = S.qord[i];
+  order_queries<NT>(
+      S, m, P.dc, s_bins, [&](int q) { return (int)(S.key[q] >> 32); },
+      [&](int q, int bk) { S.key[q] = ((unsigned long long)bk << 32) | (unsigned)S.key[q]; });
+  if (tid == 0) *s_next = 0;
+  __syncthreads();
+  for (;;) {
+    const int base = next_chunk(s_next);
+    if (base >= m) break;
+    const int i = base + lane;
+    if (i < m) {
+    const int q = (int)S.qord[i];
     const float2 pq = S.xy[q];
     const float wq = __int_as_float(S.nh[q]);
+    const bool self_in = dist2(pq, pq) <= P.t_dc;  // 0 <= t unless a coordinate is NaN
     const int bx0 = tile_bin(__fsub_rn(pq.x, P.dc)), bx1 = tile_bin(__fadd_rn(pq.x, P.dc));
     const int by0 = tile_bin(__fsub_rn(pq.y, P.dc)), by1 = tile_bin(__fadd_rn(pq.y, P.dc));
     float r = 0.f;
-    // candidates of all columns as one flattened sequence, in the reference order
-    int c = bx0 - 1, k = 0, e = 0;
+    // all columns as one flattened candidate sequence in the reference order;
+    // the query's own position splits its segment so the i == j term (w, not
+    // 0.5 w) is added exactly where the reference adds it
+    int c = bx0 - 1, k = 0, e = 0, e_after = -1;
     for (;;) {
       if (k >= e) {
+        if (e_after >= 0) {
+          if (self_in) r = __fadd_rn(r, wq);
+          k = q + 1;
+          e = e_after;
+          e_after = -1;
+          continue;
+        }
         if (++c > bx1) break;
         k = (int)S.tbl[c * kGridCols + by0];
         e = (int)S.tbl[c * kGridCols + by1 + 1];
+        if (q >= k && q < e) {
+          e_after = e;
+          e = q;
+        }
         continue;
       }
-      const float d2 = dist2(pq, S.xy[k]);
-      if (d2 <= P.t_dc) r = __fadd_rn(r, (k == q) ? wq : S.hw[k]);
+      if (dist2(pq, S.xy[k]) <= P.t_dc) r = __fadd_rn(r, S.hw[k]);
       ++k;
     }
     const unsigned g = (unsigned)S.key[q];
     b.rho[in.ev_start + g] = r;
     S.key[q] = ((unsigned long long)float_ord(r) << 32) | g;
+    }
   }
   __syncthreads();
 
   // -- distance to the nearest higher (kernel_calculate_distanceToHigher, :57-106)
   // "higher" (rho_j > rho_i, or equal rho and j > i) is key_j > key_i; a NaN
   // rho is higher than nothing and nothing is higher than it, as in the reference.
-  order_queries<NT>(S, m, P.dm, reinterpret_cast<int32_t*>(S.delta), s_bins);
-  for (int i = tid; i < m; i += NT) {
-    const int q = S.qord[i];
+  int32_t* hwi = reinterpret_cast<int32_t*>(S.hw);  // 0.5 w is not needed any more
+  order_queries<NT>(
+      S, m, P.dm, s_bins, [&](int q) { return hwi[q]; }, [&](int q, int bk) { hwi[q] = bk; });
+  if (tid == 0) *s_next = 0;
+  __syncthreads();
+  int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
+  for (;;) {
+    const int base = next_chunk(s_next);
+    if (base >= m) break;
+    const int i = base + lane;
+    if (i < m) {
+    const int q = (int)S.qord[i];
     const float2 pq = S.xy[q];
     const unsigned long long ks = S.key[q];
     const unsigned long long kq = (ks >> 32) == 0ull ? ~0ull : ks;
@@ -319,25 +403,16 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT>& S, const 
       }
       ++k;
     }
-    S.delta[q] = best_s;
-    S.nh[q] = best;
-  }
-  __syncthreads();
-
-  // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
-  int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
-  for (int q = tid; q < m; q += NT) {
-    const unsigned long long ks = S.key[q];
+    // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
     const float r = ord_float((unsigned)(ks >> 32));
-    const float d = S.delta[q];
-    const int n = S.nh[q];
-    const bool seed = (d > P.dc) && (r >= P.rhoc);
-    const bool outlier = (d > P.dm) && (r < P.rhoc);
+    const bool seed = (best_s > P.dc) && (r >= P.rhoc);
+    const bool outlier = (best_s > P.dm) && (r < P.rhoc);
     const int64_t o = in.ev_start + (unsigned)ks;
-    b.delta[o] = d;
-    b.nh[o] = n >= 0 ? (int)(unsigned)S.key[n] : -1;
+    b.delta[o] = best_s;
+    b.nh[o] = best >= 0 ? (int)(unsigned)S.key[best] : -1;
     b.seed[o] = seed ? 1 : 0;
-    par[q] = (!seed && !outlier && n >= 0) ? n : (seed ? -2 : -3);
+    par[q] = (!seed && !outlier && best >= 0) ? best : (seed ? -2 : -3);
+    }
   }
   __syncthreads();
   // -- pointer jumping along nearestHigher (replaces the follower stack, :138-152)
@@ -461,20 +536,20 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ int s_item;
+  __shared__ int s_next;
   __shared__ int s_ws[33];
   __shared__ int s_bins[64];
   const int n_items = b.n_events * kLayers;
   const bool grouped = b.flags[kFlagGrouped] != 0;
-  LayerStore<uint16_t> sm;
+  LayerStore<uint16_t, uint16_t> sm;
   sm.tbl = reinterpret_cast<uint16_t*>(dsm);
   {
-    unsigned char* p = dsm + ((kTableInts * 2 + 15) / 16) * 16;
+    unsigned char* p = dsm + kSmemTableBytes;
     sm.xy = reinterpret_cast<float2*>(p);
     sm.key = reinterpret_cast<unsigned long long*>(sm.xy + cap);
     sm.hw = reinterpret_cast<float*>(sm.key + cap);
-    sm.delta = sm.hw + cap;
-    sm.nh = reinterpret_cast<int32_t*>(sm.delta + cap);
-    sm.qord = sm.nh + cap;
+    sm.nh = reinterpret_cast<int32_t*>(sm.hw + cap);
+    sm.qord = reinterpret_cast<uint16_t*>(sm.nh + cap);
   }
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(&b.flags[kFlagTicket], 1);
@@ -503,19 +578,18 @@ __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
       io.gid_base = 0;
     }
     if (m <= cap) {
-      process_layer<NT>(P, sm, m, io, b, s_ws, s_bins);
+      process_layer<NT>(P, sm, m, io, b, s_ws, s_bins, &s_next);
     } else {
       // spill: the same stages on HBM scratch at this layer's grouped position
-      LayerStore<int32_t> g;
+      LayerStore<int32_t, int32_t> g;
       g.xy = reinterpret_cast<float2*>(b.sp[0]) + start;
       g.key = reinterpret_cast<unsigned long long*>(b.sp[2]) + start;
       g.hw = b.sp[4] + start;
-      g.delta = b.sp[5] + start;
       g.nh = reinterpret_cast<int32_t*>(b.sp[6]) + start;
       g.qord = reinterpret_cast<int32_t*>(b.sp[7]) + start;
       g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableStride;
       if (threadIdx.x == 0) atomicAdd(&b.flags[kFlagSpilled], 1);
-      process_layer<NT>(P, g, m, io, b, s_ws, s_bins);
+      process_layer<NT>(P, g, m, io, b, s_ws, s_bins, &s_next);
     }
   }
 }
@@ -631,6 +705,7 @@ cudaError_t prepare_clue2d_kernels(int device) {
   int optin = 0;
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e != cudaSuccess) return e;
+  if ((e = allow_max_smem<128>(optin)) != cudaSuccess) return e;
   if ((e = allow_max_smem<256>(optin)) != cudaSuccess) return e;
   if ((e = allow_max_smem<512>(optin)) != cudaSuccess) return e;
   return allow_max_smem<1024>(optin);
@@ -667,8 +742,8 @@ Params2D make_params2d(float dc, float rhoc, float odf) {
 }
 
 size_t layer_smem_bytes(const Tuning2D& t) {
-  // 16-bit tile table, then 32 bytes per point (see LayerStore)
-  return ((size_t)(kTableInts * 2 + 15) / 16) * 16 + (size_t)t.layer_capacity * 32;
+  // 16-bit tile table, then 26 bytes per point (see LayerStore)
+  return (size_t)kSmemTableBytes + (size_t)t.layer_capacity * 26;
 }
 
 int layer_grid(const Tuning2D& t, int n_items) {
@@ -720,6 +795,7 @@ cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t
   if (err != cudaSuccess) return err;
   mark(3);
   switch (t.threads) {
+    case 128: err = launch_layers<128>(b, p, t, s); break;
     case 256: err = launch_layers<256>(b, p, t, s); break;
     case 1024: err = launch_layers<1024>(b, p, t, s); break;
     default: err = launch_layers<512>(b, p, t, s); break;

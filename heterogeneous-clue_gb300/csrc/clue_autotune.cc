@@ -94,9 +94,9 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
     int smem_optin = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     std::vector<Tuning2D> cands;
-    const int caps[] = {1024, 1536, 2048, 3072, 4096, 6144};
-    const int threads[] = {256, 512};
-    const float tiles[] = {0.f, 2.5f};
+    const int caps[] = {1536, 2048, 3072, 4096, 6144};
+    const int threads[] = {128, 256, 512};
+    const float tiles[] = {0.f};
     for (int th : threads)
       for (int cap : caps)
         for (float wt : tiles) {

@@ -14,6 +14,8 @@ constexpr int kLayers = 100;
 constexpr int kGridCols = 100;
 constexpr int kTiles = kGridCols * kGridCols;
 constexpr int kTableInts = kTiles + 1;
+// Bytes of the on-chip 16-bit tile table (a multiple of 16).
+constexpr int kSmemTableBytes = ((kTableInts * 2 + 15) / 16) * 16;
 // Per-CTA stride of the HBM tile tables (32-bit counts), a multiple of 16 bytes.
 constexpr int kTableStride = ((kTableInts * 4 + 15) / 16) * 4;
 // Points per event-aligned chunk of the streaming kernels (count, scatter, seed ranks).
@@ -36,8 +38,8 @@ Params2D make_params2d(float dc, float rhoc, float odf);
 float sqrt_le_threshold(float d);
 
 struct Tuning2D {
-  int threads = 512;
-  int layer_capacity = 4096;
+  int threads = 256;
+  int layer_capacity = 2048;
   float work_tile_cm = 0.f;
   int ctas_per_sm = 0;
 };

@@ -623,8 +623,8 @@ int clue_get_tuning(clue_handle* hh, clue_tuning* t) {
 
 int clue_set_tuning(clue_handle* hh, const clue_tuning* t) {
   if (!hh || !t) return set_error(CLUE_EINVAL, "NULL argument");
-  if (t->threads != 256 && t->threads != 512 && t->threads != 1024)
-    return set_error(CLUE_EINVAL, "threads must be 256, 512 or 1024");
+  if (t->threads != 128 && t->threads != 256 && t->threads != 512 && t->threads != 1024)
+    return set_error(CLUE_EINVAL, "threads must be 128, 256, 512 or 1024");
   if (t->layer_capacity < 32 || clue::layer_smem_bytes(clue::Tuning2D{t->threads, t->layer_capacity}) > 227 * 1024 - 1024)
     return set_error(CLUE_EINVAL, "layer_capacity %d does not fit in shared memory", t->layer_capacity);
   if (!(t->work_tile_cm == 0.f || (t->work_tile_cm >= 0.5f && t->work_tile_cm <= 4.f)))

@@ -178,6 +178,7 @@ class Server {
     st->p99_ms = pct(0.99);
     st->mean_batch_events = batches_ ? double(batched_events_) / batches_ : 0.0;
     st->max_inflight_seen = max_inflight_seen_;
+    st->slot_capacity_points = cap_points_;
   }
 
   void reset_stats() {

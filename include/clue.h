@@ -59,7 +59,7 @@ typedef struct clue_outputs {
 
 /* Work decomposition of the batched kernels.  None of it changes results. */
 typedef struct clue_tuning {
-  int32_t threads;        /* threads per CTA of the layer kernel: 256, 512 or 1024 */
+  int32_t threads;        /* threads per CTA of the layer kernel: 128, 256, 512 or 1024 */
   int32_t layer_capacity; /* points of one layer held on-chip; larger layers use HBM scratch */
   float work_tile_cm;     /* query grouping inside a 5 cm tile: 0 (none) or 0.5 .. 4 cm */
   int32_t ctas_per_sm;    /* 0 = as many as shared memory allows */
@@ -204,6 +204,7 @@ typedef struct clue_server_stats {
   double p99_ms;
   double mean_batch_events;
   double max_inflight_seen;
+  int64_t slot_capacity_points; /* largest event (points) one in-flight batch admits */
 } clue_server_stats;
 
 int clue_server_create(const clue_params* params, const clue_server_config* cfg, clue_server** out);

@@ -86,12 +86,21 @@ def test_one_request_against_the_oracle(events):
     srv.close()
 
 
-def test_admission_rejects_an_event_larger_than_a_slot(events):
-    srv = C.Server(*PRM, budget_bytes=64 << 20, max_inflight=2, max_batch_events=4)
-    big = S.hgcal_event(1000)
+def _uniform_event(n, seed):
+    rng = np.random.default_rng(seed)
+    return dict(x=rng.uniform(-240, 240, n).astype(np.float32), y=rng.uniform(-240, 240, n).astype(np.float32),
+                layer=rng.integers(0, 100, n).astype(np.int32), weight=rng.exponential(1.0, n).astype(np.float32))
+
+
+def test_admission_rejects_an_event_larger_than_a_slot():
+    srv = C.Server(*PRM, budget_bytes=96 << 20, max_inflight=2, max_batch_events=4)
+    cap = srv.stats()["slot_capacity_points"]
+    assert cap > 1000
     with pytest.raises(C.ClueError) as ei:
-        srv.submit(**big)
+        srv.submit(**_uniform_event(cap + 1, 1))
     assert ei.value.code == C.CLUE_ENOMEM
-    rid, out = srv.submit(**events[0])  # a small one still fits
+    small = _uniform_event(cap // 2, 2)
+    rid, out = srv.submit(**small)  # half a slot still fits
     assert srv.poll(rid, timeout_ms=60000)[0] == C.CLUE_OK
+    assert_bitexact(out, oracle.clue2d(small["x"], small["y"], small["layer"], small["weight"], *PRM))
     srv.close()
