@@ -253,6 +253,33 @@ __device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const fl
   __syncthreads();
 }
 
+// Candidate sequence of a search box spanning one to three tile columns:
+// segment j is column bx0+j, rows [by0, by1], i.e. sorted positions
+// [s_j, s_j + l_j).  at(t) maps the t-th candidate of the concatenation to
+// its sorted position with compares and selects only.
+struct SegIndex {
+  int b1, b2, total, d0, d1, d2;
+  template <class TT>
+  __device__ __forceinline__ void init(const TT* tbl, int bx0, int nseg, int by0, int by1) {
+    int s[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j < nseg) {
+        const int c = (bx0 + j) * kGridCols;
+        s[j] = (int)tbl[c + by0];
+        l[j] = max(0, (int)tbl[c + by1 + 1] - s[j]);
+      }
+    }
+    b1 = l[0];
+    b2 = l[0] + l[1];
+    total = b2 + l[2];
+    d0 = s[0];
+    d1 = s[1] - b1;
+    d2 = s[2] - b2;
+  }
+  __device__ __forceinline__ int at(int t) const { return t + (t < b1 ? d0 : (t < b2 ? d1 : d2)); }
+};
+
 // Next chunk of 32 queries for this warp (dynamic, in query order).
 __device__ __forceinline__ int next_chunk(int* s_next) {
   int base = 0;
@@ -329,6 +356,20 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     const int bx0 = tile_bin(__fsub_rn(pq.x, P.dc)), bx1 = tile_bin(__fadd_rn(pq.x, P.dc));
     const int by0 = tile_bin(__fsub_rn(pq.y, P.dc)), by1 = tile_bin(__fadd_rn(pq.y, P.dc));
     float r = 0.f;
+    const int nseg = bx1 - bx0 + 1;
+    if (nseg >= 1 && nseg <= 3) {
+      // up to three column segments as one flattened sequence in the
+      // reference order; the candidate index is derived without branches so
+      // that every lane runs the same straight-line loop
+      SegIndex sg;
+      sg.init(S.tbl, bx0, nseg, by0, by1);
+#pragma unroll 2
+      for (int t = 0; t < sg.total; ++t) {
+        const int k = sg.at(t);
+        const float h = (k == q) ? wq : S.hw[k];  // the i == j term is w, not 0.5 w
+        if (dist2(pq, S.xy[k]) <= P.t_dc) r = __fadd_rn(r, h);
+      }
+    } else {
     // all columns as one flattened candidate sequence in the reference order;
     // the query's own position splits its segment so the i == j term (w, not
     // 0.5 w) is added exactly where the reference adds it
@@ -353,6 +394,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
       }
       if (dist2(pq, S.xy[k]) <= P.t_dc) r = __fadd_rn(r, S.hw[k]);
       ++k;
+    }
     }
     const unsigned g = (unsigned)S.key[q];
     b.rho[in.ev_start + g] = r;
@@ -383,14 +425,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     const int by0 = tile_bin(__fsub_rn(pq.y, P.dm)), by1 = tile_bin(__fadd_rn(pq.y, P.dm));
     float best_s = FLT_MAX, best_d2 = INFINITY;
     int best = -1;
-    int c = bx0 - 1, k = 0, e = 0;
-    for (;;) {
-      if (k >= e) {
-        if (++c > bx1) break;
-        k = (int)S.tbl[c * kGridCols + by0];
-        e = (int)S.tbl[c * kGridCols + by1 + 1];
-        continue;
-      }
+    auto visit = [&](int k) {
       const unsigned long long kk = S.key[k];
       const float d2 = dist2(pq, S.xy[k]);
       if (kk > kq && d2 <= P.t_dm && d2 < best_d2) {
@@ -401,7 +436,25 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
           best = k;
         }
       }
-      ++k;
+    };
+    const int nseg = bx1 - bx0 + 1;
+    if (nseg >= 1 && nseg <= 3) {
+      SegIndex sg;
+      sg.init(S.tbl, bx0, nseg, by0, by1);
+#pragma unroll 2
+      for (int t = 0; t < sg.total; ++t) visit(sg.at(t));
+    } else {
+      int c = bx0 - 1, k = 0, e = 0;
+      for (;;) {
+        if (k >= e) {
+          if (++c > bx1) break;
+          k = (int)S.tbl[c * kGridCols + by0];
+          e = (int)S.tbl[c * kGridCols + by1 + 1];
+          continue;
+        }
+        visit(k);
+        ++k;
+      }
     }
     // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
     const float r = ord_float((unsigned)(ks >> 32));
