@@ -184,15 +184,17 @@ __device__ __forceinline__ float ord_float(unsigned o) {
 
 // Per-layer working set, sorted by tile: on-chip for layers up to the tuned
 // capacity (16-bit table and query order), in HBM scratch beyond it (32-bit).
-// 26 bytes per point on chip plus the 20 KB table.
+// One 16-byte record per point, so a candidate is a single 128-bit load:
+//   {x, y, gid, aux}: aux = 0.5f*w (bits) during the density search and
+//   float_ord(rho) during the nearest-higher search, when the upper 8 bytes
+//   read as one 64-bit key (float_ord(rho) << 32) | gid.
+// 22 bytes per point on chip plus the 20 KB table.
 template <class TT, class QT>
 struct LayerStore {
-  float2* xy;               // position
-  unsigned long long* key;  // (float_ord(rho) << 32) | gid; gid (+ a bucket above it) before rho exists
-  float* hw;                // 0.5f * w, the reference's neighbour term
-  int32_t* nh;              // own weight (bits) during density, then the parent pointer
-  QT* qord;                 // query order of the current search
-  TT* tbl;                  // kTableInts: exclusive scan over key = xBin*100 + yBin
+  uint4* rec;
+  int32_t* nh;  // own weight (bits), then float_ord(rho), then the parent pointer
+  QT* qord;     // query order of the current search
+  TT* tbl;      // kTableInts: exclusive scan over key = xBin*100 + yBin
 };
 
 struct LayerIO {
@@ -204,37 +206,35 @@ struct LayerIO {
   int64_t ev_start;
 };
 
-__device__ __forceinline__ int candidate_count(const uint16_t* tbl, int bx0, int bx1, int by0, int by1) {
+__device__ __forceinline__ float2 rec_xy(const uint4& r) { return make_float2(__uint_as_float(r.x), __uint_as_float(r.y)); }
+__device__ __forceinline__ unsigned long long rec_key(const uint4& r) {
+  return ((unsigned long long)r.w << 32) | r.z;
+}
+
+template <class TT>
+__device__ __forceinline__ int candidate_count(const TT* tbl, int bx0, int bx1, int by0, int by1) {
   int cnt = 0;
   for (int c = bx0; c <= bx1; ++c) cnt += max(0, (int)tbl[c * kGridCols + by1 + 1] - (int)tbl[c * kGridCols + by0]);
   return cnt;
 }
-__device__ __forceinline__ int candidate_count(const int32_t* tbl, int bx0, int bx1, int by0, int by1) {
-  int cnt = 0;
-  for (int c = bx0; c <= bx1; ++c) cnt += max(0, tbl[c * kGridCols + by1 + 1] - tbl[c * kGridCols + by0]);
-  return cnt;
-}
 
 // Query order of a search phase: queries bucketed by their candidate count,
-// heaviest first; warps then take chunks of 32 in that order.  Which thread
-// runs which query never changes a result.  `bucket_of(q)` / `set_bucket`
-// park the bucket in a word the phase does not need yet.
-template <int NT, class TT, class QT, class Get, class Set>
-__device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const float d, int* s_bins, Get bucket_of,
-                              Set set_bucket) {
+// heaviest first; warps then take chunks of 32 in that order, so the lanes
+// of a warp run loops of similar length.  Which thread runs which query never
+// changes a result.  The bucket is computed twice instead of being stored.
+template <int NT, class TT, class QT>
+__device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const float d, int* s_bins) {
   constexpr int NB = 64;
   const int tid = threadIdx.x;
-  for (int i = tid; i < NB; i += NT) s_bins[i] = 0;
-  __syncthreads();
-  for (int q = tid; q < m; q += NT) {
-    const float2 p = S.xy[q];
+  auto bucket = [&](int q) {
+    const float2 p = rec_xy(S.rec[q]);
     const int bx0 = tile_bin(__fsub_rn(p.x, d)), bx1 = tile_bin(__fadd_rn(p.x, d));
     const int by0 = tile_bin(__fsub_rn(p.y, d)), by1 = tile_bin(__fadd_rn(p.y, d));
-    const int cnt = candidate_count(S.tbl, bx0, bx1, by0, by1);
-    const int bk = NB - 1 - min(cnt >> 2, NB - 1);
-    set_bucket(q, bk);
-    atomicAdd(&s_bins[bk], 1);
-  }
+    return NB - 1 - min(candidate_count(S.tbl, bx0, bx1, by0, by1) >> 2, NB - 1);
+  };
+  for (int i = tid; i < NB; i += NT) s_bins[i] = 0;
+  __syncthreads();
+  for (int q = tid; q < m; q += NT) atomicAdd(&s_bins[bucket(q)], 1);
   __syncthreads();
   if (tid < 32) {
     const int a = s_bins[2 * tid], c = s_bins[2 * tid + 1];
@@ -249,7 +249,7 @@ __device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const fl
     s_bins[2 * tid + 1] = ex + a;
   }
   __syncthreads();
-  for (int q = tid; q < m; q += NT) S.qord[atomicAdd(&s_bins[bucket_of(q)], 1)] = (QT)q;
+  for (int q = tid; q < m; q += NT) S.qord[atomicAdd(&s_bins[bucket(q)], 1)] = (QT)q;
   __syncthreads();
 }
 
@@ -258,7 +258,7 @@ __device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const fl
 // [s_j, s_j + l_j).  at(t) maps the t-th candidate of the concatenation to
 // its sorted position with compares and selects only.
 struct SegIndex {
-  int b1, b2, total, d0, d1, d2;
+  int b1 = 0, b2 = 0, total = 0, d0 = 0, d1 = 0, d2 = 0;
   template <class TT>
   __device__ __forceinline__ void init(const TT* tbl, int bx0, int nseg, int by0, int by1) {
     int s[3] = {0, 0, 0}, l[3] = {0, 0, 0};
@@ -280,6 +280,25 @@ struct SegIndex {
   __device__ __forceinline__ int at(int t) const { return t + (t < b1 ? d0 : (t < b2 ? d1 : d2)); }
 };
 
+// Visits the candidates of a search box in the reference order: the
+// branchless flattened form for boxes of up to three columns, otherwise a
+// general column loop.
+template <class TT, class F>
+__device__ __forceinline__ void for_candidates(const TT* tbl, int bx0, int bx1, int by0, int by1, F&& visit) {
+  const int nseg = bx1 - bx0 + 1;
+  if (nseg >= 1 && nseg <= 3) {
+    SegIndex sg;
+    sg.init(tbl, bx0, nseg, by0, by1);
+#pragma unroll 2
+    for (int t = 0; t < sg.total; ++t) visit(sg.at(t));
+  } else {
+    for (int c = bx0; c <= bx1; ++c) {
+      const int e = (int)tbl[c * kGridCols + by1 + 1];
+      for (int k = (int)tbl[c * kGridCols + by0]; k < e; ++k) visit(k);
+    }
+  }
+}
+
 // Next chunk of 32 queries for this warp (dynamic, in query order).
 __device__ __forceinline__ int next_chunk(int* s_next) {
   int base = 0;
@@ -293,7 +312,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   const int tid = threadIdx.x, lane = tid & 31;
   QT* kkey = S.qord;                                     // sort key, later final slot
   int32_t* kprov = S.nh;                                 // provisional slot in tile
-  int32_t* slot_p = reinterpret_cast<int32_t*>(S.key);  // input position at provisional slot
+  int32_t* slot_p = reinterpret_cast<int32_t*>(S.rec);  // input position at provisional slot
   int32_t* slot_g = slot_p + m;                          // gid at provisional slot
 
   // -- counting sort into tiles (kernel_compute_histogram, CLUEAlgoKernels.h:18-23)
@@ -331,17 +350,14 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   for (int p = tid; p < m; p += NT) {
     const int f = (int)kkey[p];
     const float wv = in.w[p];
-    S.xy[f] = make_float2(in.x[p], in.y[p]);
-    S.hw[f] = __fmul_rn(0.5f, wv);
+    const unsigned g = (unsigned)(in.gid ? in.gid[p] : in.gid_base + p);
+    S.rec[f] = make_uint4(__float_as_uint(in.x[p]), __float_as_uint(in.y[p]), g, __float_as_uint(__fmul_rn(0.5f, wv)));
     S.nh[f] = __float_as_int(wv);
-    S.key[f] = (unsigned long long)(unsigned)(in.gid ? in.gid[p] : in.gid_base + p);
   }
   __syncthreads();
 
   // -- local density (kernel_calculate_density, CLUEAlgoKernels.h:25-55)
-  order_queries<NT>(
-      S, m, P.dc, s_bins, [&](int q) { return (int)(S.key[q] >> 32); },
-      [&](int q, int bk) { S.key[q] = ((unsigned long long)bk << 32) | (unsigned)S.key[q]; });
+  order_queries<NT>(S, m, P.dc, s_bins);
   if (tid == 0) *s_next = 0;
   __syncthreads();
   for (;;) {
@@ -349,66 +365,36 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     if (base >= m) break;
     const int i = base + lane;
     if (i < m) {
-    const int q = (int)S.qord[i];
-    const float2 pq = S.xy[q];
-    const float wq = __int_as_float(S.nh[q]);
-    const bool self_in = dist2(pq, pq) <= P.t_dc;  // 0 <= t unless a coordinate is NaN
-    const int bx0 = tile_bin(__fsub_rn(pq.x, P.dc)), bx1 = tile_bin(__fadd_rn(pq.x, P.dc));
-    const int by0 = tile_bin(__fsub_rn(pq.y, P.dc)), by1 = tile_bin(__fadd_rn(pq.y, P.dc));
-    float r = 0.f;
-    const int nseg = bx1 - bx0 + 1;
-    if (nseg >= 1 && nseg <= 3) {
-      // up to three column segments as one flattened sequence in the
-      // reference order; the candidate index is derived without branches so
-      // that every lane runs the same straight-line loop
-      SegIndex sg;
-      sg.init(S.tbl, bx0, nseg, by0, by1);
-#pragma unroll 2
-      for (int t = 0; t < sg.total; ++t) {
-        const int k = sg.at(t);
-        const float h = (k == q) ? wq : S.hw[k];  // the i == j term is w, not 0.5 w
-        if (dist2(pq, S.xy[k]) <= P.t_dc) r = __fadd_rn(r, h);
-      }
-    } else {
-    // all columns as one flattened candidate sequence in the reference order;
-    // the query's own position splits its segment so the i == j term (w, not
-    // 0.5 w) is added exactly where the reference adds it
-    int c = bx0 - 1, k = 0, e = 0, e_after = -1;
-    for (;;) {
-      if (k >= e) {
-        if (e_after >= 0) {
-          if (self_in) r = __fadd_rn(r, wq);
-          k = q + 1;
-          e = e_after;
-          e_after = -1;
-          continue;
-        }
-        if (++c > bx1) break;
-        k = (int)S.tbl[c * kGridCols + by0];
-        e = (int)S.tbl[c * kGridCols + by1 + 1];
-        if (q >= k && q < e) {
-          e_after = e;
-          e = q;
-        }
-        continue;
-      }
-      if (dist2(pq, S.xy[k]) <= P.t_dc) r = __fadd_rn(r, S.hw[k]);
-      ++k;
-    }
-    }
-    const unsigned g = (unsigned)S.key[q];
-    b.rho[in.ev_start + g] = r;
-    S.key[q] = ((unsigned long long)float_ord(r) << 32) | g;
+      const int q = (int)S.qord[i];
+      const uint4 rq = S.rec[q];
+      const float2 pq = rec_xy(rq);
+      const float wq = __int_as_float(S.nh[q]);
+      const int bx0 = tile_bin(__fsub_rn(pq.x, P.dc)), bx1 = tile_bin(__fadd_rn(pq.x, P.dc));
+      const int by0 = tile_bin(__fsub_rn(pq.y, P.dc)), by1 = tile_bin(__fadd_rn(pq.y, P.dc));
+      float r = 0.f;
+      for_candidates(S.tbl, bx0, bx1, by0, by1, [&](int k) {
+        const uint4 rk = S.rec[k];
+        const float h = (k == q) ? wq : __uint_as_float(rk.w);  // the i == j term is w, not 0.5 w
+        if (dist2(pq, rec_xy(rk)) <= P.t_dc) r = __fadd_rn(r, h);
+      });
+      b.rho[in.ev_start + rq.z] = r;
+      S.nh[q] = (int)float_ord(r);  // nobody reads nh[q] during this search but this thread
     }
   }
+  __syncthreads();
+  for (int q = tid; q < m; q += NT) S.rec[q].w = (unsigned)S.nh[q];
   __syncthreads();
 
   // -- distance to the nearest higher (kernel_calculate_distanceToHigher, :57-106)
   // "higher" (rho_j > rho_i, or equal rho and j > i) is key_j > key_i; a NaN
-  // rho is higher than nothing and nothing is higher than it, as in the reference.
-  int32_t* hwi = reinterpret_cast<int32_t*>(S.hw);  // 0.5 w is not needed any more
-  order_queries<NT>(
-      S, m, P.dm, s_bins, [&](int q) { return hwi[q]; }, [&](int q, int bk) { hwi[q] = bk; });
+  // rho is higher than nothing and nothing is higher than it, as in the
+  // reference.  The winner is the first candidate with the smallest
+  // correctly rounded sqrt(d2).  The loop keeps the first candidate with the
+  // smallest d2 and takes the exact sqrt comparison only for near ties:
+  //   d2 < 0.99999 * best_d2  implies  sqrt_rn(d2) < sqrt_rn(best_d2),
+  // so a candidate below `lim` always wins, one at or above best_d2 never
+  // does (sqrt_rn is monotone), and one in between is decided by sqrt_rn.
+  order_queries<NT>(S, m, P.dm, s_bins);
   if (tid == 0) *s_next = 0;
   __syncthreads();
   int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
@@ -417,54 +403,41 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     if (base >= m) break;
     const int i = base + lane;
     if (i < m) {
-    const int q = (int)S.qord[i];
-    const float2 pq = S.xy[q];
-    const unsigned long long ks = S.key[q];
-    const unsigned long long kq = (ks >> 32) == 0ull ? ~0ull : ks;
-    const int bx0 = tile_bin(__fsub_rn(pq.x, P.dm)), bx1 = tile_bin(__fadd_rn(pq.x, P.dm));
-    const int by0 = tile_bin(__fsub_rn(pq.y, P.dm)), by1 = tile_bin(__fadd_rn(pq.y, P.dm));
-    float best_s = FLT_MAX, best_d2 = INFINITY;
-    int best = -1;
-    auto visit = [&](int k) {
-      const unsigned long long kk = S.key[k];
-      const float d2 = dist2(pq, S.xy[k]);
-      if (kk > kq && d2 <= P.t_dm && d2 < best_d2) {
-        const float sd = __fsqrt_rn(d2);
-        if (sd < best_s) {
-          best_s = sd;
-          best_d2 = d2;
-          best = k;
+      const int q = (int)S.qord[i];
+      const uint4 rq = S.rec[q];
+      const float2 pq = rec_xy(rq);
+      const unsigned long long ks = rec_key(rq);
+      const unsigned long long kq = rq.w == 0u ? ~0ull : ks;
+      const int bx0 = tile_bin(__fsub_rn(pq.x, P.dm)), bx1 = tile_bin(__fadd_rn(pq.x, P.dm));
+      const int by0 = tile_bin(__fsub_rn(pq.y, P.dm)), by1 = tile_bin(__fadd_rn(pq.y, P.dm));
+      float best_d2 = P.t_dm_next, lim = P.t_dm_next;  // d2 < t_dm_next <=> d2 <= t_dm
+      int best = -1;
+      for_candidates(S.tbl, bx0, bx1, by0, by1, [&](int k) {
+        const uint4 rk = S.rec[k];
+        const float d2 = dist2(pq, rec_xy(rk));
+        const bool higher = rec_key(rk) > kq;
+        const bool win = higher && d2 < lim;
+        if (higher && !win && d2 < best_d2) {  // near tie: rare
+          if (__fsqrt_rn(d2) < __fsqrt_rn(best_d2)) {
+            best = k;
+            best_d2 = d2;
+            lim = __fmul_rn(d2, 0.99999f);
+          }
         }
-      }
-    };
-    const int nseg = bx1 - bx0 + 1;
-    if (nseg >= 1 && nseg <= 3) {
-      SegIndex sg;
-      sg.init(S.tbl, bx0, nseg, by0, by1);
-#pragma unroll 2
-      for (int t = 0; t < sg.total; ++t) visit(sg.at(t));
-    } else {
-      int c = bx0 - 1, k = 0, e = 0;
-      for (;;) {
-        if (k >= e) {
-          if (++c > bx1) break;
-          k = (int)S.tbl[c * kGridCols + by0];
-          e = (int)S.tbl[c * kGridCols + by1 + 1];
-          continue;
-        }
-        visit(k);
-        ++k;
-      }
-    }
-    // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
-    const float r = ord_float((unsigned)(ks >> 32));
-    const bool seed = (best_s > P.dc) && (r >= P.rhoc);
-    const bool outlier = (best_s > P.dm) && (r < P.rhoc);
-    const int64_t o = in.ev_start + (unsigned)ks;
-    b.delta[o] = best_s;
-    b.nh[o] = best >= 0 ? (int)(unsigned)S.key[best] : -1;
-    b.seed[o] = seed ? 1 : 0;
-    par[q] = (!seed && !outlier && best >= 0) ? best : (seed ? -2 : -3);
+        best = win ? k : best;
+        best_d2 = win ? d2 : best_d2;
+        lim = win ? __fmul_rn(d2, 0.99999f) : lim;
+      });
+      const float best_s = best >= 0 ? __fsqrt_rn(best_d2) : FLT_MAX;
+      // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
+      const float r = ord_float(rq.w);
+      const bool seed = (best_s > P.dc) && (r >= P.rhoc);
+      const bool outlier = (best_s > P.dm) && (r < P.rhoc);
+      const int64_t o = in.ev_start + rq.z;
+      b.delta[o] = best_s;
+      b.nh[o] = best >= 0 ? (int)S.rec[best].z : -1;
+      b.seed[o] = seed ? 1 : 0;
+      par[q] = (!seed && !outlier && best >= 0) ? best : (seed ? -2 : -3);
     }
   }
   __syncthreads();
@@ -487,7 +460,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     const int p = par[q];
     const int root = p >= 0 ? p : q;
     // seed roots carry their event-local index until k_seed_rank/k_label
-    b.ci[in.ev_start + (unsigned)S.key[q]] = (par[root] == -2) ? (int)(unsigned)S.key[root] : -1;
+    b.ci[in.ev_start + S.rec[q].z] = (par[root] == -2) ? (int)S.rec[root].z : -1;
   }
   __syncthreads();
 }
@@ -586,7 +559,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
+__global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P, int cap) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ int s_item;
   __shared__ int s_next;
@@ -596,14 +569,9 @@ __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
   const bool grouped = b.flags[kFlagGrouped] != 0;
   LayerStore<uint16_t, uint16_t> sm;
   sm.tbl = reinterpret_cast<uint16_t*>(dsm);
-  {
-    unsigned char* p = dsm + kSmemTableBytes;
-    sm.xy = reinterpret_cast<float2*>(p);
-    sm.key = reinterpret_cast<unsigned long long*>(sm.xy + cap);
-    sm.hw = reinterpret_cast<float*>(sm.key + cap);
-    sm.nh = reinterpret_cast<int32_t*>(sm.hw + cap);
-    sm.qord = reinterpret_cast<uint16_t*>(sm.nh + cap);
-  }
+  sm.rec = reinterpret_cast<uint4*>(dsm + kSmemTableBytes);
+  sm.nh = reinterpret_cast<int32_t*>(sm.rec + cap);
+  sm.qord = reinterpret_cast<uint16_t*>(sm.nh + cap);
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(&b.flags[kFlagTicket], 1);
     __syncthreads();
@@ -635,11 +603,9 @@ __global__ void __launch_bounds__(NT) k_layers(Batch2D b, Params2D P, int cap) {
     } else {
       // spill: the same stages on HBM scratch at this layer's grouped position
       LayerStore<int32_t, int32_t> g;
-      g.xy = reinterpret_cast<float2*>(b.sp[0]) + start;
-      g.key = reinterpret_cast<unsigned long long*>(b.sp[2]) + start;
-      g.hw = b.sp[4] + start;
-      g.nh = reinterpret_cast<int32_t*>(b.sp[6]) + start;
-      g.qord = reinterpret_cast<int32_t*>(b.sp[7]) + start;
+      g.rec = reinterpret_cast<uint4*>(b.sp[0]) + start;
+      g.nh = reinterpret_cast<int32_t*>(b.sp[4]) + start;
+      g.qord = reinterpret_cast<int32_t*>(b.sp[5]) + start;
       g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableStride;
       if (threadIdx.x == 0) atomicAdd(&b.flags[kFlagSpilled], 1);
       process_layer<NT>(P, g, m, io, b, s_ws, s_bins, &s_next);
@@ -791,12 +757,14 @@ Params2D make_params2d(float dc, float rhoc, float odf) {
   p.dm = a * c;
   p.t_dc = sqrt_le_threshold(dc);
   p.t_dm = sqrt_le_threshold(p.dm);
+  // the next float above t_dm (d2 < t_dm_next <=> d2 <= t_dm); -1 stays -1
+  p.t_dm_next = p.t_dm < 0.f ? p.t_dm : nextafterf(p.t_dm, INFINITY);
   return p;
 }
 
 size_t layer_smem_bytes(const Tuning2D& t) {
-  // 16-bit tile table, then 26 bytes per point (see LayerStore)
-  return (size_t)kSmemTableBytes + (size_t)t.layer_capacity * 26;
+  // 16-bit tile table, then 22 bytes per point (see LayerStore)
+  return (size_t)kSmemTableBytes + (size_t)t.layer_capacity * 22;
 }
 
 int layer_grid(const Tuning2D& t, int n_items) {

@@ -30,6 +30,7 @@ struct Params2D {
   float dm;    // odf * dc, as the reference computes it (float product)
   float t_dc;  // largest float t >= 0 with sqrtf(t) <= dc, or -1 when none
   float t_dm;  // same for dm
+  float t_dm_next;  // next float above t_dm (or -1)
 };
 
 // Host: fill Params2D from the three reference parameters.

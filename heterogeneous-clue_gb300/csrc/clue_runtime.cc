@@ -119,10 +119,10 @@ std::vector<size_t> sizes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bo
   s[S_CS] = 4 * (size_t)(E + 1);
   s[S_LCNT] = s[S_LSTART] = s[S_CURSOR] = 4 * (size_t)E * kLayers;
   s[S_GX] = s[S_GY] = s[S_GW] = s[S_GID] = 4 * (size_t)N;
-  // spill homes: xy (8 B), key (8 B), then hw, delta, nh, qord (4 B each)
-  s[S_SP0] = s[S_SP2] = 8 * (size_t)N;
-  s[S_SP1] = s[S_SP3] = 0;
-  s[S_SP4] = s[S_SP5] = s[S_SP6] = s[S_SP7] = 4 * (size_t)N;
+  // spill homes: 16-byte records, then nh and the query order (4 B each)
+  s[S_SP0] = 16 * (size_t)N;
+  s[S_SP1] = s[S_SP2] = s[S_SP3] = s[S_SP6] = s[S_SP7] = 0;
+  s[S_SP4] = s[S_SP5] = 4 * (size_t)N;
   s[S_SPTBL] = 4 * (size_t)kTableStride * grid;
   s[S_CSEED] = s[S_CBASE] = 4 * (size_t)std::max<int64_t>(nchunks, 1);
   s[S_FLAGS] = 4 * kFlagCount;
