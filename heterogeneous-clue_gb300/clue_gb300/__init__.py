@@ -121,6 +121,8 @@ def lib():
         "clue_set_tuning": ([H, ctypes.POINTER(Tuning)], ctypes.c_int),
         "clue_autotune": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), ctypes.c_char_p,
                            ctypes.POINTER(Tuning)], ctypes.c_int),
+        "clue_run_event_noalloc": ([ctypes.POINTER(Params), ctypes.c_int32, _vp, _vp, _vp, _vp,
+                                    ctypes.POINTER(Outputs), _vp], ctypes.c_int),
         "clue3d_default_params": ([ctypes.POINTER(Params3D)], None),
         "clue3d_run_batch": ([H, ctypes.POINTER(Params3D), ctypes.c_int32, _i64p, ctypes.POINTER(Inputs3D),
                               ctypes.POINTER(Outputs3D), _i32p, ctypes.c_int], ctypes.c_int),

@@ -123,6 +123,23 @@ int clue_autotune(clue_handle* h, int32_t n_events, const int64_t* event_offsets
 
 const char* clue_last_error(void);
 
+/* One event through the batched kernels WITHOUT allocating anything: no
+ * handle, no cudaMalloc/cudaFree, no allocating library call.  It has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory themselves (a host framework that pre-reserves the whole
+ * device for its own pool, real-time or embedded code that must not touch
+ * the allocator after start-up).  x, y, layer, weight and the outputs are
+ * DEVICE pointers; work runs on cuda_stream (NULL = default stream) and the
+ * call synchronises that stream before returning.
+ * Scratch is one fixed 14 MB area compiled into the library (a static
+ * __device__ array that every GPU using the library holds until the process
+ * exits), so n is limited to 262,144 points; larger events get CLUE_EINVAL.
+ * The first call on a device looks up the area's address (make it before
+ * any stream capture).  All calls share the area: calls that overlap on the
+ * GPU race; run them one at a time. */
+int clue_run_event_noalloc(const clue_params* params, int32_t n, const float* x, const float* y,
+                           const int32_t* layer, const float* weight, const clue_outputs* out, void* cuda_stream);
+
 /* ------------------------------------------------------------------------ */
 /* CLUE3D (tracksterizer)                                                     */
 /* ------------------------------------------------------------------------ */
