@@ -286,7 +286,31 @@ struct SegIndex {
 template <class TT, class F>
 __device__ __forceinline__ void for_candidates(const TT* tbl, int bx0, int bx1, int by0, int by1, F&& visit) {
   const int nseg = bx1 - bx0 + 1;
-  if (nseg >= 1 && nseg <= 3) {
+  // the widest box among the active lanes picks the loop form for the warp,
+  // so that lanes never split between two loops
+  const unsigned act = __activemask();
+  const bool any3 = __any_sync(act, nseg == 3);
+  const bool anywide = __any_sync(act, nseg > 3);
+  if (!any3 && !anywide) {
+    // one or two columns (every density box when dc < 2.5 cm): one compare
+    // and one select per candidate
+    int b1 = 0, total = 0, d0 = 0, d1 = 0;
+    if (nseg >= 1) {
+      const int s0 = (int)tbl[bx0 * kGridCols + by0];
+      const int l0 = max(0, (int)tbl[bx0 * kGridCols + by1 + 1] - s0);
+      int s1 = 0, l1 = 0;
+      if (nseg == 2) {
+        s1 = (int)tbl[(bx0 + 1) * kGridCols + by0];
+        l1 = max(0, (int)tbl[(bx0 + 1) * kGridCols + by1 + 1] - s1);
+      }
+      b1 = l0;
+      total = l0 + l1;
+      d0 = s0;
+      d1 = s1 - l0;
+    }
+#pragma unroll 2
+    for (int t = 0; t < total; ++t) visit(t + (t < b1 ? d0 : d1));
+  } else if (!anywide) {
     SegIndex sg;
     sg.init(tbl, bx0, nseg, by0, by1);
 #pragma unroll 2
@@ -410,25 +434,37 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
       const unsigned long long kq = rq.w == 0u ? ~0ull : ks;
       const int bx0 = tile_bin(__fsub_rn(pq.x, P.dm)), bx1 = tile_bin(__fadd_rn(pq.x, P.dm));
       const int by0 = tile_bin(__fsub_rn(pq.y, P.dm)), by1 = tile_bin(__fadd_rn(pq.y, P.dm));
-      float best_d2 = P.t_dm_next, lim = P.t_dm_next;  // d2 < t_dm_next <=> d2 <= t_dm
+      float best_d2 = P.t_dm_next;  // d2 < t_dm_next <=> d2 <= t_dm
       int best = -1;
+      bool near = false;
       for_candidates(S.tbl, bx0, bx1, by0, by1, [&](int k) {
         const uint4 rk = S.rec[k];
         const float d2 = dist2(pq, rec_xy(rk));
-        const bool higher = rec_key(rk) > kq;
-        const bool win = higher && d2 < lim;
-        if (higher && !win && d2 < best_d2) {  // near tie: rare
-          if (__fsqrt_rn(d2) < __fsqrt_rn(best_d2)) {
-            best = k;
-            best_d2 = d2;
-            lim = __fmul_rn(d2, 0.99999f);
-          }
-        }
+        const bool imp = (rec_key(rk) > kq) && d2 < best_d2;
+        // d2 * 1.00002 < best_d2 guarantees sqrt_rn(d2) < sqrt_rn(best_d2)
+        const bool win = imp && __fmul_rn(d2, 1.00002f) < best_d2;
+        near |= imp && !win;
         best = win ? k : best;
         best_d2 = win ? d2 : best_d2;
-        lim = win ? __fmul_rn(d2, 0.99999f) : lim;
       });
-      const float best_s = best >= 0 ? __fsqrt_rn(best_d2) : FLT_MAX;
+      float best_s = best >= 0 ? __fsqrt_rn(best_d2) : FLT_MAX;
+      if (near) {
+        // a candidate came within the margin of the running best: decide this
+        // query again with the reference's comparison on sqrt'd distances
+        best_s = FLT_MAX;
+        best = -1;
+        for_candidates(S.tbl, bx0, bx1, by0, by1, [&](int k) {
+          const uint4 rk = S.rec[k];
+          const float d2 = dist2(pq, rec_xy(rk));
+          if (rec_key(rk) > kq && d2 <= P.t_dm) {
+            const float sd = __fsqrt_rn(d2);
+            if (sd < best_s) {
+              best_s = sd;
+              best = k;
+            }
+          }
+        });
+      }
       // -- seeds, outliers, outputs (kernel_findAndAssign_clusters, :108-136)
       const float r = ord_float(rq.w);
       const bool seed = (best_s > P.dc) && (r >= P.rhoc);
