@@ -38,6 +38,10 @@ BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
 STAGES_PER_STEP = 8
+# DRAM bytes per point of one k_layers launch, from the ncu capture summarised in
+# profiles/k_layers_uneven256.md (read + write over 13.6M points); traffic grows
+# with the point count, so a full launch is scaled by its points.
+K_LAYERS_DRAM_BYTES_PER_POINT = 28.05
 
 
 def _dist():
@@ -54,15 +58,6 @@ def _peak_hbm():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
-
-
-def _traffic(name):
-    p = os.path.join(ROOT, "profiles", name)
-    try:
-        with open(p) as f:
-            return json.load(f)
-    except Exception:
-        return None
 
 
 class ClockSampler:
@@ -191,6 +186,88 @@ def _config(args, b):
             "l2": "inputs (16 B/point) larger than L2; no flush"}
 
 
+def serving_leg(C, b, rate, n_req, batched=True):
+    """Poisson arrivals of events from the workload at ``rate`` events/s into
+    the continuous-batching server (batched) or into a one-event-per-launch
+    server (plain: one batch of one event in flight); latency is submit ->
+    outputs written, measured by the server."""
+    import numpy as np
+
+    from clue_gb300 import synthetic as S
+    E = b["offsets"].size - 1
+    rng = np.random.default_rng(5)
+    idx = rng.integers(0, E, n_req)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    views = [S.event_of(b, int(e)) for e in idx]
+    srv = C.Server(*PARAMS, budget_bytes=16 << 30, max_inflight=2 if batched else 1,
+                   max_batch_events=256 if batched else 1)
+    # warm the slots (allocation, first launches) outside the measurement
+    warm = [srv.submit(**views[i]) for i in range(min(8, n_req))]
+    srv.drain()
+    for rid, _ in warm:
+        srv.poll(rid, 0)
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    ids = []
+    for i in range(n_req):
+        target = t0 + arrivals[i]
+        while True:
+            now = time.perf_counter()
+            if now >= target:
+                break
+            if target - now > 0.002:
+                time.sleep(target - now - 0.001)
+        ids.append(srv.submit(**views[i]))
+    srv.drain()
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    for rid, _ in ids:
+        srv.poll(rid, 0)
+    srv.close()
+    pts = sum(int(v["x"].size) for v in views)
+    return {"offered_events_per_s": rate, "requests": n_req, "achieved_events_per_s": n_req / elapsed,
+            "achieved_gpoints_per_s": pts / elapsed / 1e9, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "mean_batch_events": st["mean_batch_events"], "max_inflight_seen": st["max_inflight_seen"],
+            "budget_bytes": 16 << 30, "max_inflight": 2 if batched else 1}
+
+
+def clue3d_leg(C, torch, stream, args):
+    """Batched CLUE3D on synthetic layer clusters: 1000 events of 2k-20k
+    clusters, 100 layers, +-2 sibling layers, criticalDensity 0.5."""
+    import numpy as np
+
+    from clue_gb300 import synthetic as S
+    b3 = S.clue3d_batch(args.clue3d_events, seed0=1000, n_layers=100)
+    off = b3["offsets"]
+    n = int(off[-1])
+    prm = dict(n_layers=100, density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)
+    fields = ("z", "eta", "phi", "r_over_absz", "radius", "layer", "energy", "isSilicon")
+    dev = {k: torch.from_numpy(np.ascontiguousarray(b3[k])).cuda() for k in fields}
+    out = {k: torch.empty(n, dtype=torch.float32 if k in ("rho", "delta_transverse") else torch.int32,
+                          device="cuda")
+           for k in ("rho", "delta_transverse", "delta_layers", "nh_layer", "nh_index", "isSeed", "tracksterIndex")}
+    algo = C.Clusterizer(*PARAMS, budget_bytes=32 << 30, stream=stream.cuda_stream)
+    for _ in range(2):
+        algo.run_clue3d(off, dev, params=prm, flags=C.DEVICE_MEMORY, out=out)
+    algo.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(3, args.steps)
+    e0.record(stream)
+    for _ in range(steps):
+        algo.run_clue3d(off, dev, params=prm, flags=C.DEVICE_MEMORY, out=out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    algo.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    algo.close()
+    peak, _ = _peak_hbm()
+    achieved = 92 * n / (ms / 1000.0) / 1e9
+    return {"events": int(off.size - 1), "layer_clusters": n, "ms_per_step": ms,
+            "events_per_s": (off.size - 1) / (ms / 1000.0), "mclusters_per_s": n / (ms / 1000.0) / 1e6,
+            "params": prm, "roofline": {"algorithmic_bytes_per_cluster": 92, "achieved_gbs": achieved,
+                                        "peak_gbs": peak, "frac": achieved / peak}}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -228,11 +305,7 @@ def run_gb300(args):
             torch.distributed.barrier()
 
     def max_over_ranks(v):
-        if ws > 1:
-            t = torch.tensor([v], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return C.dist_max(v, device="cuda")
 
     def run(flags):
         algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
@@ -269,10 +342,7 @@ def run_gb300(args):
     layers_ms = stage_ms["layers"]
     achieved = BYTES_PER_POINT * N / (layers_ms / 1000.0) / 1e9
     pipe_achieved = BYTES_PER_POINT * N / (ms_step / 1000.0) / 1e9
-    tr = _traffic("k_layers_traffic.json")
-    traffic = None
-    if tr and tr.get("bytes_per_point"):
-        traffic = tr["bytes_per_point"] * N
+    traffic = K_LAYERS_DRAM_BYTES_PER_POINT * N
     roofline = {"bound": "hbm", "kernel": "k_layers", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_point": BYTES_PER_POINT,
@@ -315,6 +385,15 @@ def run_gb300(args):
                "h2d_bytes_per_step": 16 * N + 12 * (E + 1), "d2h_bytes_per_step": 20 * N + 32,
                "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps}
 
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = {"batched": serving_leg(C, b, args.serving_rate, args.serving_requests, batched=True),
+                   "plain": serving_leg(C, b, args.serving_rate, max(200, args.serving_requests // 4),
+                                        batched=False)}
+    clue3d = None
+    if rank == 0 and not args.no_clue3d:
+        clue3d = clue3d_leg(C, torch, stream, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -331,6 +410,7 @@ def run_gb300(args):
                 "config": _config(args, b), "gpoints_per_s": gpts,
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
                 "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "serving": serving, "clue3d": clue3d,
                 "clocks": clk.summary(), "gpu_launches": STAGES_PER_STEP * args.steps,
                 "tuning": algo.get_tuning()}
         print(json.dumps(line), flush=True)
@@ -354,6 +434,11 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-rate", type=float, default=2000.0)
+    ap.add_argument("--serving-requests", type=int, default=3000)
+    ap.add_argument("--no-clue3d", action="store_true")
+    ap.add_argument("--clue3d-events", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -353,3 +353,50 @@ class Server:
 
     def reset_stats(self):
         check(lib().clue_server_reset_stats(self._s))
+
+
+# ----------------------------------------------------------------------------
+# Multi-process helpers (events are independent: ranks shard them, no collective
+# touches the data path)
+# ----------------------------------------------------------------------------
+
+def shard_events(offsets, rank, world):
+    """Contiguous event range [e0, e1) of ``rank`` among ``world`` ranks,
+    balanced by point count; the ranges cover every event exactly once."""
+    offsets = np.asarray(offsets, np.int64)
+    E = offsets.size - 1
+    N = int(offsets[-1])
+    if world <= 1:
+        return 0, E
+
+    def bound(r):
+        if r <= 0:
+            return 0
+        if r >= world:
+            return E
+        return int(min(E, np.searchsorted(offsets[:-1], (N * r) // world, side="left")))
+
+    return bound(rank), bound(rank + 1)
+
+
+def shard_batch(batch, rank, world):
+    """The sub-batch (rebased offsets and array views) of ``rank``'s shard."""
+    e0, e1 = shard_events(batch["offsets"], rank, world)
+    off = batch["offsets"]
+    s, t = int(off[e0]), int(off[e1])
+    out = {k: batch[k][s:t] for k in ("x", "y", "layer", "weight")}
+    out["offsets"] = (off[e0:e1 + 1] - off[e0]).astype(np.int64)
+    out["event_range"] = (e0, e1)
+    return out
+
+
+def dist_max(value, device=None):
+    """Max of a float over the ranks of the default process group (gloo or
+    nccl); the value itself when no group is initialised."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
