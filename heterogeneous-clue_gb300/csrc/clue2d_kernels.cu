@@ -147,12 +147,12 @@ __device__ void block_scan_table(uint16_t* tbl, int n, int* s_ws) {
 
 // Histogram increment returning the previous count.  The on-chip table holds
 // 16-bit counts (a layer there has < 65536 points), two per 32-bit word.
-__device__ __forceinline__ int hist_add(uint16_t* t, int key) {
+__device__ __forceinline__ int hist_add(uint16_t* t, int key, int n) {
   unsigned* w = reinterpret_cast<unsigned*>(t) + (key >> 1);
   const int sh = (key & 1) * 16;
-  return (int)((atomicAdd(w, 1u << sh) >> sh) & 0xffffu);
+  return (int)((atomicAdd(w, (unsigned)n << sh) >> sh) & 0xffffu);
 }
-__device__ __forceinline__ int hist_add(int32_t* t, int key) { return atomicAdd(t + key, 1); }
+__device__ __forceinline__ int hist_add(int32_t* t, int key, int n) { return atomicAdd(t + key, n); }
 
 // Squared distance dx*dx + dy*dy with the reference's rounding: two
 // correctly rounded differences, two correctly rounded squares (computed as
@@ -346,31 +346,58 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     for (int i = tid; i < kTableBytes / 16; i += NT) t4[i] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();
-  for (int p = tid; p < m; p += NT) {
-    const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
-    kkey[p] = (QT)key;
-    kprov[p] = hist_add(S.tbl, key);
+  if (!in.gid) {
+    // Input already in index order (points of an event grouped by layer):
+    // one warp walks it in order and gives each point its rank among the
+    // earlier points of its tile, i.e. its final place -- a stable counting
+    // sort, no rank restore needed.
+    if (tid < 32) {
+      const unsigned lt = (1u << lane) - 1u;
+      for (int base = 0; base < m; base += 32) {
+        const int p = base + lane;
+        const int key = p < m ? tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]) : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(grp) - 1;
+        int old = 0;
+        if (key >= 0 && lane == leader) old = hist_add(S.tbl, key, __popc(grp));
+        old = __shfl_sync(0xffffffffu, old, leader);
+        if (key >= 0) {
+          kkey[p] = (QT)key;
+          kprov[p] = old + __popc(grp & lt);
+        }
+      }
+    }
+    __syncthreads();
+    block_scan_table<NT>(S.tbl, kTiles, s_ws);
+    for (int p = tid; p < m; p += NT) kkey[p] = (QT)((int)S.tbl[kkey[p]] + kprov[p]);
+    __syncthreads();
+  } else {
+    for (int p = tid; p < m; p += NT) {
+      const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
+      kkey[p] = (QT)key;
+      kprov[p] = hist_add(S.tbl, key, 1);
+    }
+    __syncthreads();
+    block_scan_table<NT>(S.tbl, kTiles, s_ws);
+    for (int p = tid; p < m; p += NT) {
+      const int q = (int)S.tbl[kkey[p]] + kprov[p];
+      slot_g[q] = in.gid[p];
+      slot_p[q] = p;
+    }
+    __syncthreads();
+    // Atomics gave an arbitrary order inside a tile; the reference appends in
+    // index order, so place each point at its gid rank within the tile.
+    for (int q = tid; q < m; q += NT) {
+      const int p = slot_p[q];
+      const int key = (int)kkey[p];
+      const int s = (int)S.tbl[key], e = (int)S.tbl[key + 1];
+      const int g = slot_g[q];
+      int rank = 0;
+      for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
+      kkey[p] = (QT)(s + rank);
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  block_scan_table<NT>(S.tbl, kTiles, s_ws);
-  for (int p = tid; p < m; p += NT) {
-    const int q = (int)S.tbl[kkey[p]] + kprov[p];
-    slot_g[q] = in.gid ? in.gid[p] : in.gid_base + p;
-    slot_p[q] = p;
-  }
-  __syncthreads();
-  // Atomics gave an arbitrary order inside a tile; the reference appends in
-  // index order, so place each point at its gid rank within the tile.
-  for (int q = tid; q < m; q += NT) {
-    const int p = slot_p[q];
-    const int key = (int)kkey[p];
-    const int s = (int)S.tbl[key], e = (int)S.tbl[key + 1];
-    const int g = slot_g[q];
-    int rank = 0;
-    for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
-    kkey[p] = (QT)(s + rank);
-  }
-  __syncthreads();
   for (int p = tid; p < m; p += NT) {
     const int f = (int)kkey[p];
     const float wv = in.w[p];
@@ -380,8 +407,11 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   }
   __syncthreads();
 
+  // One query order for both searches, by the nearest-higher box (the
+  // larger box and the more expensive search).
+  order_queries<NT>(S, m, P.dm, s_bins);
+
   // -- local density (kernel_calculate_density, CLUEAlgoKernels.h:25-55)
-  order_queries<NT>(S, m, P.dc, s_bins);
   if (tid == 0) *s_next = 0;
   __syncthreads();
   for (;;) {
@@ -418,7 +448,6 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   //   d2 < 0.99999 * best_d2  implies  sqrt_rn(d2) < sqrt_rn(best_d2),
   // so a candidate below `lim` always wins, one at or above best_d2 never
   // does (sqrt_rn is monotone), and one in between is decided by sqrt_rn.
-  order_queries<NT>(S, m, P.dm, s_bins);
   if (tid == 0) *s_next = 0;
   __syncthreads();
   int32_t* par = S.nh;  // parent: nearest higher for followers, -2 seed root, -3 other root
@@ -477,26 +506,42 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     }
   }
   __syncthreads();
-  // -- pointer jumping along nearestHigher (replaces the follower stack, :138-152)
-  for (;;) {
-    int changed = 0;
-    for (int q = tid; q < m; q += NT) {
-      const int p = par[q];
-      if (p >= 0) {
-        const int pp = par[p];
-        if (pp >= 0) {
-          par[q] = pp;
-          changed = 1;
+  // -- roots of the nearestHigher chains (replaces the follower stack,
+  // :138-152): each point walks its chain; chains longer than 64 steps are
+  // finished by pointer jumping.
+  QT* root = S.qord;  // the query order is not needed any more
+  int unresolved = 0;
+  for (int q = tid; q < m; q += NT) {
+    int r = q, p = par[q];
+    for (int step = 0; p >= 0 && step < 64; ++step) {
+      r = p;
+      p = par[r];
+    }
+    root[q] = (QT)r;
+    unresolved |= (p >= 0);
+  }
+  if (__syncthreads_or(unresolved)) {
+    for (;;) {
+      int changed = 0;
+      for (int q = tid; q < m; q += NT) {
+        const int p = par[q];
+        if (p >= 0) {
+          const int pp = par[p];
+          if (pp >= 0) {
+            par[q] = pp;
+            changed = 1;
+          }
         }
       }
+      if (!__syncthreads_or(changed)) break;
     }
-    if (!__syncthreads_or(changed)) break;
+    for (int q = tid; q < m; q += NT) root[q] = (QT)(par[q] >= 0 ? par[q] : q);
+    __syncthreads();
   }
   for (int q = tid; q < m; q += NT) {
-    const int p = par[q];
-    const int root = p >= 0 ? p : q;
+    const int r = (int)root[q];
     // seed roots carry their event-local index until k_seed_rank/k_label
-    b.ci[in.ev_start + S.rec[q].z] = (par[root] == -2) ? (int)S.rec[root].z : -1;
+    b.ci[in.ev_start + S.rec[q].z] = (par[r] == -2) ? (int)S.rec[r].z : -1;
   }
   __syncthreads();
 }
