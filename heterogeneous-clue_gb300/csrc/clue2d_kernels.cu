@@ -346,32 +346,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     for (int i = tid; i < kTableBytes / 16; i += NT) t4[i] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();
-  if (!in.gid) {
-    // Input already in index order (points of an event grouped by layer):
-    // one warp walks it in order and gives each point its rank among the
-    // earlier points of its tile, i.e. its final place -- a stable counting
-    // sort, no rank restore needed.
-    if (tid < 32) {
-      const unsigned lt = (1u << lane) - 1u;
-      for (int base = 0; base < m; base += 32) {
-        const int p = base + lane;
-        const int key = p < m ? tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]) : -1;
-        const unsigned grp = __match_any_sync(0xffffffffu, key);
-        const int leader = __ffs(grp) - 1;
-        int old = 0;
-        if (key >= 0 && lane == leader) old = hist_add(S.tbl, key, __popc(grp));
-        old = __shfl_sync(0xffffffffu, old, leader);
-        if (key >= 0) {
-          kkey[p] = (QT)key;
-          kprov[p] = old + __popc(grp & lt);
-        }
-      }
-    }
-    __syncthreads();
-    block_scan_table<NT>(S.tbl, kTiles, s_ws);
-    for (int p = tid; p < m; p += NT) kkey[p] = (QT)((int)S.tbl[kkey[p]] + kprov[p]);
-    __syncthreads();
-  } else {
+  {
     for (int p = tid; p < m; p += NT) {
       const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
       kkey[p] = (QT)key;
@@ -381,7 +356,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     block_scan_table<NT>(S.tbl, kTiles, s_ws);
     for (int p = tid; p < m; p += NT) {
       const int q = (int)S.tbl[kkey[p]] + kprov[p];
-      slot_g[q] = in.gid[p];
+      slot_g[q] = in.gid ? in.gid[p] : in.gid_base + p;
       slot_p[q] = p;
     }
     __syncthreads();
