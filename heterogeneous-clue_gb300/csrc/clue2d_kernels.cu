@@ -308,7 +308,7 @@ __device__ __forceinline__ void for_candidates(const TT* tbl, int bx0, int bx1, 
       d0 = s0;
       d1 = s1 - l0;
     }
-#pragma unroll 2
+#pragma unroll 4
     for (int t = 0; t < total; ++t) visit(t + (t < b1 ? d0 : d1));
   } else if (!anywide) {
     SegIndex sg;
@@ -347,10 +347,19 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   }
   __syncthreads();
   {
-    for (int p = tid; p < m; p += NT) {
-      const int key = tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]);
-      kkey[p] = (QT)key;
-      kprov[p] = hist_add(S.tbl, key, 1);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int base = 0; base < m; base += NT) {
+      const int p = base + tid;
+      const int key = p < m ? tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]) : -1;
+      const unsigned grp = __match_any_sync(0xffffffffu, key);
+      const int leader = __ffs(grp) - 1;
+      int old = 0;
+      if (key >= 0 && lane == leader) old = hist_add(S.tbl, key, __popc(grp));
+      old = __shfl_sync(0xffffffffu, old, leader);
+      if (key >= 0) {
+        kkey[p] = (QT)key;
+        kprov[p] = old + __popc(grp & lt);
+      }
     }
     __syncthreads();
     block_scan_table<NT>(S.tbl, kTiles, s_ws);
