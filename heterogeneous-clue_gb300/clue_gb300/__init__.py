@@ -49,7 +49,8 @@ class Outputs(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("layer_capacity", ctypes.c_int32),
-                ("work_tile_cm", ctypes.c_float), ("ctas_per_sm", ctypes.c_int32)]
+                ("work_tile_cm", ctypes.c_float), ("ctas_per_sm", ctypes.c_int32),
+                ("big_threads", ctypes.c_int32), ("big_capacity", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

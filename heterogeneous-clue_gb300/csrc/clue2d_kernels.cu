@@ -32,6 +32,7 @@
 //    (CLUEAlgoKernels.h:114-131) and labels follow nearestHigher chains
 //    exactly where the reference's follower stack walks (:133-152).
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -623,8 +624,14 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
   }
 }
 
+// Persistent CTAs over the (event, layer) queue.  Two classes of layers: the
+// first pass (big_pass = 0) takes every item from an atomic ticket and
+// handles layers of at most max_m points on chip with `cap` points of shared
+// memory (several CTAs per SM); larger layers are appended to a list that the
+// second pass (big_pass = 1, launched with a large `cap` and fewer CTAs per
+// SM) drains.  Layers above `cap` in either pass use HBM scratch.
 template <int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P, int cap) {
+__global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P, int cap, int max_m, int big_pass) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ int s_item;
   __shared__ int s_next;
@@ -637,14 +644,27 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   sm.rec = reinterpret_cast<uint4*>(dsm + kSmemTableBytes);
   sm.nh = reinterpret_cast<int32_t*>(sm.rec + cap);
   sm.qord = reinterpret_cast<uint16_t*>(sm.nh + cap);
+  int32_t* big_list = b.cursor;  // k_scatter's cursors are dead by now
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(&b.flags[kFlagTicket], 1);
+    if (threadIdx.x == 0) {
+      if (!big_pass) {
+        const int t = atomicAdd(&b.flags[kFlagTicket], 1);
+        s_item = t < n_items ? t : -1;
+      } else {
+        const int t = atomicAdd(&b.flags[kFlagTicket2], 1);
+        s_item = t < b.flags[kFlagBigCount] ? big_list[t] : -1;
+      }
+    }
     __syncthreads();
     const int item = s_item;
     __syncthreads();
-    if (item >= n_items) break;
+    if (item < 0) break;
     const int m = b.lcnt[item];
     if (m == 0) continue;
+    if (m > max_m) {  // first pass: leave it to the large-capacity pass
+      if (threadIdx.x == 0) big_list[atomicAdd(&b.flags[kFlagBigCount], 1)] = item;
+      continue;
+    }
     const int e = item / kLayers;
     const int64_t es = b.offsets[e];
     const int start = b.lstart[item];
@@ -767,11 +787,22 @@ __global__ void __launch_bounds__(kChunkThreads) k_label(Batch2D b) {
 }
 
 template <int NT>
-cudaError_t launch_layers(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s) {
-  const size_t smem = layer_smem_bytes(t);
-  const int grid = layer_grid(t, b.n_events * kLayers);
-  k_layers<NT><<<grid, NT, smem, s>>>(b, p, t.layer_capacity);
+cudaError_t launch_layers(const Batch2D& b, const Params2D& p, int cap, int max_m, int big_pass, int grid,
+                          cudaStream_t s) {
+  Tuning2D t;
+  t.layer_capacity = cap;
+  k_layers<NT><<<grid, NT, layer_smem_bytes(t), s>>>(b, p, cap, max_m, big_pass);
   return cudaGetLastError();
+}
+
+cudaError_t launch_layers_any(int threads, const Batch2D& b, const Params2D& p, int cap, int max_m, int big_pass,
+                              int grid, cudaStream_t s) {
+  switch (threads) {
+    case 128: return launch_layers<128>(b, p, cap, max_m, big_pass, grid, s);
+    case 256: return launch_layers<256>(b, p, cap, max_m, big_pass, grid, s);
+    case 1024: return launch_layers<1024>(b, p, cap, max_m, big_pass, grid, s);
+    default: return launch_layers<512>(b, p, cap, max_m, big_pass, grid, s);
+  }
 }
 
 template <int NT>
@@ -832,6 +863,18 @@ size_t layer_smem_bytes(const Tuning2D& t) {
   return (size_t)kSmemTableBytes + (size_t)t.layer_capacity * 22;
 }
 
+int layer_grid_max(const Tuning2D& t, int n_items) {
+  int g = layer_grid(t, n_items);
+  if (t.big_threads > 0 && t.big_capacity > t.layer_capacity) {
+    Tuning2D big;
+    big.threads = t.big_threads;
+    big.layer_capacity = t.big_capacity;
+    const int g2 = layer_grid(big, n_items);
+    g = g2 > g ? g2 : g;
+  }
+  return g;
+}
+
 int layer_grid(const Tuning2D& t, int n_items) {
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
@@ -880,11 +923,17 @@ cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   mark(3);
-  switch (t.threads) {
-    case 128: err = launch_layers<128>(b, p, t, s); break;
-    case 256: err = launch_layers<256>(b, p, t, s); break;
-    case 1024: err = launch_layers<1024>(b, p, t, s); break;
-    default: err = launch_layers<512>(b, p, t, s); break;
+  {
+    const int n_items = b.n_events * kLayers;
+    const bool two_class = t.big_threads > 0 && t.big_capacity > t.layer_capacity;
+    err = launch_layers_any(t.threads, b, p, t.layer_capacity, two_class ? t.layer_capacity : INT_MAX, 0,
+                            layer_grid(t, n_items), s);
+    if (err == cudaSuccess && two_class) {
+      Tuning2D big;
+      big.threads = t.big_threads;
+      big.layer_capacity = t.big_capacity;
+      err = launch_layers_any(t.big_threads, b, p, t.big_capacity, INT_MAX, 1, layer_grid(big, n_items), s);
+    }
   }
   if (err != cudaSuccess) return err;
   mark(4);

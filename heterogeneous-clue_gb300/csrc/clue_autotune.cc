@@ -94,7 +94,7 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
     int smem_optin = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     std::vector<Tuning2D> cands;
-    const int caps[] = {1536, 2048, 3072, 4096, 6144};
+    const int caps[] = {1024, 1536, 2048, 2560};
     const int threads[] = {128, 256, 512};
     const float tiles[] = {0.f};
     for (int th : threads)
@@ -105,6 +105,8 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
           t.layer_capacity = cap;
           t.work_tile_cm = wt;
           t.ctas_per_sm = 0;
+          t.big_threads = h->tuning.big_threads;
+          t.big_capacity = h->tuning.big_capacity;
           if (layer_smem_bytes(t) + 1024 > (size_t)smem_optin) continue;
           cands.push_back(t);
         }

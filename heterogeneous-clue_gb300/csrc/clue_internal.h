@@ -23,7 +23,15 @@ constexpr int kChunk = 4096;
 constexpr int kChunkThreads = 512;
 
 // Device-side status words of one run.
-enum FlagSlot : int { kFlagGrouped = 0, kFlagError = 1, kFlagTicket = 2, kFlagSpilled = 3, kFlagCount = 8 };
+enum FlagSlot : int {
+  kFlagGrouped = 0,
+  kFlagError = 1,
+  kFlagTicket = 2,
+  kFlagSpilled = 3,
+  kFlagTicket2 = 4,   // ticket of the large-layer pass
+  kFlagBigCount = 5,  // layers left to the large-layer pass
+  kFlagCount = 8
+};
 
 struct Params2D {
   float dc, rhoc, odf;
@@ -40,9 +48,11 @@ float sqrt_le_threshold(float d);
 
 struct Tuning2D {
   int threads = 256;
-  int layer_capacity = 2048;
+  int layer_capacity = 1536;
   float work_tile_cm = 0.f;
   int ctas_per_sm = 0;
+  int big_threads = 512;     // second pass for layers above layer_capacity (0 = none)
+  int big_capacity = 8192;
 };
 
 // Device views of one 2D batch.  All [N] arrays are in the caller's point order
@@ -79,6 +89,8 @@ struct Batch2D {
 
 // Grid of the layer kernel for a tuning (needs the current device).
 int layer_grid(const Tuning2D& t, int n_items);
+// The larger grid of the two layer passes (sizes the per-CTA HBM tables).
+int layer_grid_max(const Tuning2D& t, int n_items);
 size_t layer_smem_bytes(const Tuning2D& t);
 
 // Opts the layer kernels into the device's full shared memory (once per

@@ -282,7 +282,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   int rc = h->wait_previous();
   if (rc) return rc;
   const int64_t nchunks = n_chunks_of(r.E, r.off);
-  const int grid = layer_grid(h->tuning, std::max(1, r.E * kLayers));
+  const int grid = layer_grid_max(h->tuning, std::max(1, r.E * kLayers));
   rc = h->arena.reserve(sizes_2d(r.E, r.N, nchunks, grid, host_io), h->budget);
   if (rc) return rc;
   // offsets + chunk table through pinned staging (graph nodes copy from it)
@@ -310,6 +310,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   cudaError_t e;
   if (use_graph) {
     GraphKey key{r.E, r.N, r.flags, h->tuning.threads, h->tuning.layer_capacity, h->tuning.ctas_per_sm,
+                 h->tuning.big_threads, h->tuning.big_capacity,
                  h->tuning.work_tile_cm, h->p2d.dc, h->p2d.rhoc, h->p2d.odf,
                  {(const void*)r.x, (const void*)r.y, (const void*)r.layer, (const void*)r.w,
                   (const void*)r.out->rho, (const void*)r.out->delta, (const void*)r.out->nearestHigher,
@@ -365,7 +366,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   int64_t maxn = 0;
   for (int32_t e = 0; e < r.E; ++e) maxn = std::max(maxn, r.off[e + 1] - r.off[e]);
   const int64_t maxchunks = (maxn + kChunk - 1) / kChunk;
-  const int grid = layer_grid(h->tuning, kLayers);
+  const int grid = layer_grid_max(h->tuning, kLayers);
   auto need = sizes_2d(1, maxn, maxchunks, grid, false);
   if (host_io) {
     for (int s = S_IN_X; s <= S_OUT_CI; ++s) need[s] = 4 * (size_t)maxn;
@@ -618,6 +619,8 @@ int clue_get_tuning(clue_handle* hh, clue_tuning* t) {
   t->layer_capacity = h->tuning.layer_capacity;
   t->work_tile_cm = h->tuning.work_tile_cm;
   t->ctas_per_sm = h->tuning.ctas_per_sm;
+  t->big_threads = h->tuning.big_threads;
+  t->big_capacity = h->tuning.big_capacity;
   return CLUE_OK;
 }
 
@@ -630,11 +633,19 @@ int clue_set_tuning(clue_handle* hh, const clue_tuning* t) {
   if (!(t->work_tile_cm == 0.f || (t->work_tile_cm >= 0.5f && t->work_tile_cm <= 4.f)))
     return set_error(CLUE_EINVAL, "work_tile_cm must be 0 or in [0.5, 4]");
   if (t->ctas_per_sm < 0 || t->ctas_per_sm > 8) return set_error(CLUE_EINVAL, "ctas_per_sm must be in [0, 8]");
+  if (t->big_threads != 0 && t->big_threads != 128 && t->big_threads != 256 && t->big_threads != 512 &&
+      t->big_threads != 1024)
+    return set_error(CLUE_EINVAL, "big_threads must be 0, 128, 256, 512 or 1024");
+  if (t->big_threads != 0 &&
+      clue::layer_smem_bytes(clue::Tuning2D{t->big_threads, t->big_capacity}) > 227 * 1024 - 1024)
+    return set_error(CLUE_EINVAL, "big_capacity %d does not fit in shared memory", t->big_capacity);
   Handle* h = reinterpret_cast<Handle*>(hh);
   h->tuning.threads = t->threads;
   h->tuning.layer_capacity = t->layer_capacity;
   h->tuning.work_tile_cm = t->work_tile_cm;
   h->tuning.ctas_per_sm = t->ctas_per_sm;
+  h->tuning.big_threads = t->big_threads;
+  h->tuning.big_capacity = t->big_capacity;
   return CLUE_OK;
 }
 

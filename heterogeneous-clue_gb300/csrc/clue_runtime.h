@@ -46,12 +46,13 @@ struct GraphKey {
   int32_t E = -1;
   int64_t N = -1;
   int flags = 0;
-  int threads = 0, cap = 0, ctas = 0;
+  int threads = 0, cap = 0, ctas = 0, big_threads = 0, big_cap = 0;
   float work_tile = 0.f;
   float dc = 0.f, rhoc = 0.f, odf = 0.f;
   const void* ptrs[13] = {};
   bool operator==(const GraphKey& o) const {
     if (E != o.E || N != o.N || flags != o.flags || threads != o.threads || cap != o.cap || ctas != o.ctas ||
+        big_threads != o.big_threads || big_cap != o.big_cap ||
         work_tile != o.work_tile || dc != o.dc || rhoc != o.rhoc || odf != o.odf)
       return false;
     for (int i = 0; i < 13; ++i)

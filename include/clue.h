@@ -63,6 +63,8 @@ typedef struct clue_tuning {
   int32_t layer_capacity; /* points of one layer held on-chip; larger layers use HBM scratch */
   float work_tile_cm;     /* query grouping inside a 5 cm tile: 0 (none) or 0.5 .. 4 cm */
   int32_t ctas_per_sm;    /* 0 = as many as shared memory allows */
+  int32_t big_threads;    /* second pass for layers above layer_capacity: threads per CTA, 0 = none */
+  int32_t big_capacity;   /* on-chip points of that pass; larger layers use HBM scratch */
 } clue_tuning;
 
 typedef struct clue_handle clue_handle;

@@ -127,12 +127,15 @@ def test_graph_replay_is_stable(algo):
         assert_bitexact(o, want)
 
 
-def test_spill_path_matches(algo):
-    """Layers larger than the on-chip capacity go through HBM scratch."""
+@pytest.mark.parametrize("cap,big_threads,big_cap", [(256, 0, 0), (256, 512, 1024), (1024, 256, 2048)])
+def test_spill_and_two_class_paths_match(algo, cap, big_threads, big_cap):
+    """Layers above the first pass's capacity go to the large-layer pass, and
+    layers above that pass's capacity (or all of them with no second pass)
+    through HBM scratch."""
     ev = S.hgcal_event(1002)
     t = algo.get_tuning()
     try:
-        algo.set_tuning(layer_capacity=256)
+        algo.set_tuning(layer_capacity=cap, big_threads=big_threads, big_capacity=max(big_cap, 64))
         got = algo.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
     finally:
         algo.set_tuning(**t)
