@@ -75,6 +75,18 @@ class Outputs3D(ctypes.Structure):
                                    "tracksterIndex")]
 
 
+class BridgeParams(ctypes.Structure):
+    _fields_ = [("n_layers", ctypes.c_int32), ("layer_z", _vp), ("radius", ctypes.c_float),
+                ("isSilicon", ctypes.c_int32)]
+
+
+LAYER_CLUSTER_FIELDS = ("x", "y", "z", "eta", "phi", "r_over_absz", "radius", "layer", "energy", "isSilicon")
+
+
+class LayerClusters(ctypes.Structure):
+    _fields_ = [(k, _vp) for k in LAYER_CLUSTER_FIELDS]
+
+
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int32),
                 ("max_batch_events", ctypes.c_int32), ("device", ctypes.c_int32)]
@@ -110,6 +122,7 @@ def lib():
         "clue_create": ([ctypes.POINTER(Params), ctypes.c_size_t, ctypes.c_int, _vp, ctypes.POINTER(H)], ctypes.c_int),
         "clue_destroy": ([H], ctypes.c_int),
         "clue_set_params": ([H, ctypes.POINTER(Params)], ctypes.c_int),
+        "clue_set_stream": ([H, _vp], ctypes.c_int),
         "clue_run_event": ([H, ctypes.c_int32, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), ctypes.c_int],
                            ctypes.c_int),
         "clue_run_batch": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), ctypes.c_int],
@@ -127,11 +140,16 @@ def lib():
         "clue3d_default_params": ([ctypes.POINTER(Params3D)], None),
         "clue3d_run_batch": ([H, ctypes.POINTER(Params3D), ctypes.c_int32, _i64p, ctypes.POINTER(Inputs3D),
                               ctypes.POINTER(Outputs3D), _i32p, ctypes.c_int], ctypes.c_int),
+        "clue_bridge_count": ([H, ctypes.c_int32, _i64p, _vp, _i64p], ctypes.c_int),
+        "clue_bridge_build": ([H, ctypes.POINTER(BridgeParams), ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _i64p, ctypes.POINTER(LayerClusters)], ctypes.c_int),
         "clue_server_create": ([ctypes.POINTER(Params), ctypes.POINTER(ServerConfig), ctypes.POINTER(H)],
                                ctypes.c_int),
         "clue_server_destroy": ([H], ctypes.c_int),
         "clue_server_submit": ([H, ctypes.c_int32, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), _i64p],
                                ctypes.c_int),
+        "clue_server_submit_many": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), _i64p],
+                                    ctypes.c_int),
         "clue_server_poll": ([H, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "clue_server_drain": ([H, ctypes.c_int32], ctypes.c_int),
         "clue_server_get_stats": ([H, ctypes.POINTER(ServerStats)], ctypes.c_int),
@@ -206,6 +224,11 @@ class Clusterizer:
 
     def set_params(self, dc, rhoc, outlierDeltaFactor):
         check(lib().clue_set_params(self._h, ctypes.byref(Params(dc, rhoc, outlierDeltaFactor))))
+
+    def set_stream(self, stream=None):
+        """Run later work on ``stream`` (a cudaStream_t as an int, e.g.
+        ``torch.cuda.Stream().cuda_stream``); None: the handle's own stream."""
+        check(lib().clue_set_stream(self._h, stream))
 
     def make_clusters(self, x, y, layer, weight, flags=HOST_MEMORY):
         """One event, host arrays in, host arrays out."""
@@ -291,6 +314,30 @@ class Clusterizer:
         return out, nt[:offsets.size - 1]
 
 
+    def layer_clusters(self, offsets, x, y, layer, weight, out2d, layer_z=None, radius=2.0, is_silicon=1):
+        """2D -> 3D bridge on the device: the layer clusters of a clustered
+        2D batch (CUDA tensors in ``x, y, layer, weight`` and ``out2d``) as
+        CLUE3D input.  Returns (cluster_offsets, dict of CUDA tensors); feed
+        them to ``run_clue3d(cluster_offsets, clusters, flags=DEVICE_MEMORY)``."""
+        import torch
+        from .synthetic import layer_z as default_layer_z
+        offsets = _c(offsets, np.int64)
+        E = offsets.size - 1
+        coff = np.zeros(E + 1, np.int64)
+        check(lib().clue_bridge_count(self._h, E, offsets.ctypes.data_as(_i64p), _ptr(out2d["isSeed"]),
+                                      coff.ctypes.data_as(_i64p)))
+        lz = _c(default_layer_z() if layer_z is None else layer_z, np.float32)
+        C = int(coff[-1])
+        out = {k: torch.empty(C, dtype=torch.int32 if k in ("layer", "isSilicon") else torch.float32,
+                              device=x.device) for k in LAYER_CLUSTER_FIELDS}
+        prm = BridgeParams(lz.size, lz.ctypes.data, radius, is_silicon)
+        lc = LayerClusters(*[_ptr(out[k]) if C else None for k in LAYER_CLUSTER_FIELDS])
+        check(lib().clue_bridge_build(self._h, ctypes.byref(prm), E, offsets.ctypes.data_as(_i64p), _ptr(x), _ptr(y),
+                                      _ptr(layer), _ptr(weight), _ptr(out2d["isSeed"]), _ptr(out2d["clusterIndex"]),
+                                      coff.ctypes.data_as(_i64p), ctypes.byref(lc)))
+        return coff, out
+
+
 def default_params3d():
     p = Params3D()
     lib().clue3d_default_params(ctypes.byref(p))
@@ -333,6 +380,22 @@ class Server:
                                        ctypes.byref(rid)))
         self._keep[rid.value] = out
         return rid.value, out
+
+    def submit_many(self, offsets, x, y, layer, weight):
+        """Queue several events (CSR ``offsets`` over host arrays) at once so
+        that they can share a batch.  Returns a list of (request id, outputs)."""
+        offsets = _c(offsets, np.int64)
+        x, y, w = _c(x, np.float32), _c(y, np.float32), _c(weight, np.float32)
+        layer = _c(layer, np.int32)
+        E = offsets.size - 1
+        outs = [empty_outputs(int(offsets[e + 1] - offsets[e])) for e in range(E)]
+        arr = (Outputs * max(E, 1))(*[outputs_struct(o) for o in outs])
+        ids = np.zeros(max(E, 1), np.int64)
+        check(lib().clue_server_submit_many(self._s, E, offsets.ctypes.data_as(_i64p), _ptr(x), _ptr(y), _ptr(layer),
+                                            _ptr(w), arr, ids.ctypes.data_as(_i64p)))
+        for e in range(E):
+            self._keep[int(ids[e])] = outs[e]
+        return [(int(ids[e]), outs[e]) for e in range(E)]
 
     def poll(self, rid, timeout_ms=-1):
         """(status, latency_ms): status CLUE_OK when done, CLUE_EBUSY/ETIMEOUT otherwise."""

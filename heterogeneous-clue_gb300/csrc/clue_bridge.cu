@@ -1,0 +1,248 @@
+// 2D -> 3D bridge: the layer clusters of a clustered 2D batch, built on the
+// device as CLUE3D input (a ClusterCollection per event,
+// src/serial/DataFormats/ClusterCollection.h:6-19).  The reference has no such
+// step (its CLUE3D reads raw3D files, src/serial/bin/Source.cc:43-60), so the
+// definition is this file's:
+//
+//   * layer cluster c of event e = the 2D points with clusterIndex == c; the
+//     clusters of an event keep the 2D ids' order (seed rank in index order);
+//   * energy = sum of the weights, position = weight-weighted mean of x, y.
+//     The sums are exact fixed-point integers (weights in units of 2^-24,
+//     weight * coordinate in units of 2^-16, both rounded to nearest), so
+//     they do not depend on the order of accumulation and the GPU result is
+//     deterministic; the division and conversions are IEEE double;
+//   * layer = the seed's layer, z = layer_z[layer], r = |(x, y)|,
+//     r_over_absz = r / |z|, eta = asinh(z / max(r, 1e-9)), phi = atan2(y, x),
+//     radius and isSilicon constant.  Clusters with zero total weight take the
+//     seed's position.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "clue_runtime.h"
+
+namespace clue {
+namespace {
+
+constexpr double kWScale = 16777216.0;  // 2^24
+constexpr double kPScale = 65536.0;     // 2^16
+
+enum BridgeSlot { B_OFF, B_COFF, B_COUNT, B_ACC, B_SEED, B_LZ, B_FLAGS, B_SLOTS };
+
+__device__ __forceinline__ int32_t event_of(const int64_t* __restrict__ off, int32_t E, int64_t i) {
+  int32_t lo = 0, hi = E;  // largest e < E with off[e] <= i
+  while (hi - lo > 1) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_bridge_count(int32_t E, int64_t N, const int64_t* __restrict__ off,
+                               const int32_t* __restrict__ seed, int32_t* __restrict__ counts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    if (seed[i]) atomicAdd(&counts[event_of(off, E, i)], 1);
+}
+
+__global__ void k_bridge_accumulate(int32_t E, int64_t N, const int64_t* __restrict__ off,
+                                    const int64_t* __restrict__ coff, const float* __restrict__ x,
+                                    const float* __restrict__ y, const float* __restrict__ w,
+                                    const int32_t* __restrict__ seed, const int32_t* __restrict__ ci,
+                                    unsigned long long* __restrict__ acc, int32_t* __restrict__ seed_of,
+                                    int32_t* __restrict__ flags) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = ci[i];
+    if (c < 0) continue;
+    const int32_t e = event_of(off, E, i);
+    if (c >= coff[e + 1] - coff[e]) {
+      atomicExch(&flags[kFlagError], 1);
+      continue;
+    }
+    const int64_t g = coff[e] + c;
+    const double wd = (double)w[i];
+    atomicAdd(&acc[3 * g], (unsigned long long)__double2ll_rn(wd * kWScale));
+    atomicAdd(&acc[3 * g + 1], (unsigned long long)__double2ll_rn(wd * (double)x[i] * kPScale));
+    atomicAdd(&acc[3 * g + 2], (unsigned long long)__double2ll_rn(wd * (double)y[i] * kPScale));
+    if (seed[i]) seed_of[g] = (int32_t)i;
+  }
+}
+
+__global__ void k_bridge_finalize(int64_t C, const unsigned long long* __restrict__ acc,
+                                  const int32_t* __restrict__ seed_of, const float* __restrict__ x,
+                                  const float* __restrict__ y, const int32_t* __restrict__ layer,
+                                  const float* __restrict__ layer_z, int32_t n_layers, float radius, int32_t sil,
+                                  clue_layer_clusters o, int32_t* __restrict__ flags) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < C; g += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t s = seed_of[g];
+    int32_t L = layer[s];
+    if (L < 0 || L >= n_layers) {
+      atomicExch(&flags[kFlagError], 2);
+      L = 0;
+    }
+    const long long sw = (long long)acc[3 * g];
+    float xb, yb;
+    if (sw != 0) {
+      const double den = (double)sw;
+      xb = __double2float_rn((double)(long long)acc[3 * g + 1] * (kWScale / kPScale) / den);
+      yb = __double2float_rn((double)(long long)acc[3 * g + 2] * (kWScale / kPScale) / den);
+    } else {
+      xb = x[s];
+      yb = y[s];
+    }
+    const float z = layer_z[L];
+    const double xd = xb, yd = yb;
+    const double r = sqrt(xd * xd + yd * yd);
+    o.x[g] = xb;
+    o.y[g] = yb;
+    o.z[g] = z;
+    o.r_over_absz[g] = __double2float_rn(r / fabs((double)z));
+    o.eta[g] = __double2float_rn(asinh((double)z / fmax(r, 1e-9)));
+    o.phi[g] = __double2float_rn(atan2(yd, xd));
+    o.radius[g] = radius;
+    o.layer[g] = L;
+    o.energy[g] = __double2float_rn((double)sw / kWScale);
+    o.isSilicon[g] = sil;
+  }
+}
+
+int check_offsets(int32_t E, const int64_t* off, const char* what) {
+  if (E < 0) return set_error(CLUE_EINVAL, "n_events < 0");
+  if (E == 0) return CLUE_OK;
+  if (!off) return set_error(CLUE_EINVAL, "%s is NULL", what);
+  if (off[0] != 0) return set_error(CLUE_EINVAL, "%s[0] must be 0", what);
+  for (int32_t e = 0; e < E; ++e)
+    if (off[e + 1] < off[e]) return set_error(CLUE_EINVAL, "%s must be non-decreasing", what);
+  if (off[E] > INT32_MAX) return set_error(CLUE_EINVAL, "more than 2^31-1 entries in %s", what);
+  return CLUE_OK;
+}
+
+int grid_for(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+}
+
+size_t bridge_budget(const Handle* h) {
+  const size_t used = h->arena.total() + h->arena3d.total();
+  return h->budget > used ? h->budget - used : 0;
+}
+
+}  // namespace
+}  // namespace clue
+
+using clue::Handle;
+using clue::cuda_error;
+using clue::set_error;
+
+extern "C" {
+
+int clue_bridge_count(clue_handle* hh, int32_t E, const int64_t* off, const int32_t* isSeed,
+                      int64_t* cluster_offsets) {
+  if (!hh || !cluster_offsets) return set_error(CLUE_EINVAL, "NULL argument");
+  int rc = clue::check_offsets(E, off, "event_offsets");
+  if (rc) return rc;
+  cluster_offsets[0] = 0;
+  if (E == 0) return CLUE_OK;
+  const int64_t N = off[E];
+  if (N > 0 && !isSeed) return set_error(CLUE_EINVAL, "isSeed is NULL");
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  if ((rc = h->wait_previous())) return rc;
+  std::vector<size_t> need(clue::B_SLOTS, 0);
+  need[clue::B_OFF] = 8 * (size_t)(E + 1);
+  need[clue::B_COUNT] = 4 * (size_t)E;
+  if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
+  if ((rc = h->stage.reserve(8 * (size_t)(E + 1)))) return rc;
+  auto P = [&](int s) { return h->arena_bridge.ptr(s); };
+  cudaStream_t s = h->stream;
+  memcpy(h->stage.p, off, 8 * (size_t)(E + 1));
+  if ((e = cudaMemcpyAsync(P(clue::B_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemsetAsync(P(clue::B_COUNT), 0, 4 * (size_t)E, s)))
+    return cuda_error(e, "bridge set-up");
+  if (N > 0)
+    clue::k_bridge_count<<<clue::grid_for(N), 256, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
+                                                            isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
+  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_count");
+  std::vector<int32_t> counts(E);
+  if ((e = cudaMemcpyAsync(counts.data(), P(clue::B_COUNT), 4 * (size_t)E, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return cuda_error(e, "bridge counts");
+  for (int32_t i = 0; i < E; ++i) cluster_offsets[i + 1] = cluster_offsets[i] + counts[i];
+  return CLUE_OK;
+}
+
+int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, const int64_t* off, const float* x,
+                      const float* y, const int32_t* layer, const float* weight, const int32_t* isSeed,
+                      const int32_t* clusterIndex, const int64_t* coff, const clue_layer_clusters* out) {
+  if (!hh || !p || !out) return set_error(CLUE_EINVAL, "NULL argument");
+  int rc = clue::check_offsets(E, off, "event_offsets");
+  if (rc) return rc;
+  if ((rc = clue::check_offsets(E, coff, "cluster_offsets"))) return rc;
+  if (p->n_layers < 1 || !p->layer_z) return set_error(CLUE_EINVAL, "bridge needs n_layers >= 1 and a z table");
+  if (E == 0) return CLUE_OK;
+  const int64_t N = off[E], C = coff[E];
+  if (N > 0 && (!x || !y || !layer || !weight || !isSeed || !clusterIndex))
+    return set_error(CLUE_EINVAL, "NULL input array");
+  const void* outs[10] = {out->x, out->y, out->z, out->eta, out->phi, out->r_over_absz, out->radius,
+                          out->layer, out->energy, out->isSilicon};
+  if (C > 0)
+    for (auto q : outs)
+      if (!q) return set_error(CLUE_EINVAL, "NULL output array");
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  if ((rc = h->wait_previous())) return rc;
+  std::vector<size_t> need(clue::B_SLOTS, 0);
+  need[clue::B_OFF] = need[clue::B_COFF] = 8 * (size_t)(E + 1);
+  need[clue::B_COUNT] = 4 * (size_t)E;
+  need[clue::B_ACC] = 24 * (size_t)std::max<int64_t>(C, 1);
+  need[clue::B_SEED] = 4 * (size_t)std::max<int64_t>(C, 1);
+  need[clue::B_LZ] = 4 * (size_t)p->n_layers;
+  need[clue::B_FLAGS] = 4 * clue::kFlagCount;
+  if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
+  const size_t stage_bytes = 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers;
+  if ((rc = h->stage.reserve(stage_bytes))) return rc;
+  if ((rc = h->flags_host.reserve(4 * clue::kFlagCount))) return rc;
+  auto P = [&](int s) { return h->arena_bridge.ptr(s); };
+  char* st = static_cast<char*>(h->stage.p);
+  memcpy(st, off, 8 * (size_t)(E + 1));
+  memcpy(st + 8 * (size_t)(E + 1), coff, 8 * (size_t)(E + 1));
+  memcpy(st + 16 * (size_t)(E + 1), p->layer_z, 4 * (size_t)p->n_layers);
+  cudaStream_t s = h->stream;
+  if ((e = cudaMemcpyAsync(P(clue::B_OFF), st, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemcpyAsync(P(clue::B_COFF), st + 8 * (size_t)(E + 1), 8 * (size_t)(E + 1), cudaMemcpyHostToDevice,
+                           s)) ||
+      (e = cudaMemcpyAsync(P(clue::B_LZ), st + 16 * (size_t)(E + 1), 4 * (size_t)p->n_layers,
+                           cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemsetAsync(P(clue::B_ACC), 0, 24 * (size_t)std::max<int64_t>(C, 1), s)) ||
+      (e = cudaMemsetAsync(P(clue::B_SEED), 0, 4 * (size_t)std::max<int64_t>(C, 1), s)) ||
+      (e = cudaMemsetAsync(P(clue::B_FLAGS), 0, 4 * clue::kFlagCount, s)))
+    return cuda_error(e, "bridge set-up");
+  int32_t* flags = static_cast<int32_t*>(P(clue::B_FLAGS));
+  auto* acc = static_cast<unsigned long long*>(P(clue::B_ACC));
+  auto* seed_of = static_cast<int32_t*>(P(clue::B_SEED));
+  if (N > 0)
+    clue::k_bridge_accumulate<<<clue::grid_for(N), 256, 0, s>>>(
+        E, N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int64_t*>(P(clue::B_COFF)), x, y,
+        weight, isSeed, clusterIndex, acc, seed_of, flags);
+  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_accumulate");
+  if (C > 0)
+    clue::k_bridge_finalize<<<clue::grid_for(C), 256, 0, s>>>(C, acc, seed_of, x, y, layer,
+                                                               static_cast<const float*>(P(clue::B_LZ)),
+                                                               p->n_layers, p->radius, p->isSilicon, *out, flags);
+  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_finalize");
+  if ((e = cudaMemcpyAsync(h->flags_host.p, flags, 4 * clue::kFlagCount, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return cuda_error(e, "bridge");
+  int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
+  const int32_t err = fh[clue::kFlagError];
+  fh[clue::kFlagError] = 0;
+  if (err == 1) return set_error(CLUE_EINVAL, "a clusterIndex is not below its event's cluster count");
+  if (err == 2) return set_error(CLUE_EINVAL, "a layer cluster's layer is outside [0, %d)", p->n_layers);
+  return CLUE_OK;
+}
+
+}  // extern "C"

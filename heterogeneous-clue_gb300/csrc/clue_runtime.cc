@@ -155,7 +155,7 @@ Handle::~Handle() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (done_event) cudaEventDestroy(done_event);
   arena.release();
-  if (own_stream && stream) cudaStreamDestroy(stream);
+  if (owned_stream) cudaStreamDestroy(owned_stream);
 }
 
 int Handle::wait_previous() {
@@ -540,14 +540,13 @@ int clue_create(const clue_params* params, size_t budget, int device, void* stre
   h->p2d = clue::make_params2d(params->dc, params->rhoc, params->outlierDeltaFactor);
   if (stream) {
     h->stream = static_cast<cudaStream_t>(stream);
-    h->own_stream = false;
   } else {
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
       delete h;
       return cuda_error(e, "cudaStreamCreate");
     }
-    h->own_stream = true;
+    h->owned_stream = h->stream;
   }
   e = cudaEventCreateWithFlags(&h->done_event, cudaEventDisableTiming);
   if (e != cudaSuccess) {
@@ -564,6 +563,28 @@ int clue_destroy(clue_handle* hh) {
   cudaSetDevice(h->device);
   if (h->pending) cudaEventSynchronize(h->done_event);
   delete h;
+  return CLUE_OK;
+}
+
+int clue_set_stream(clue_handle* hh, void* stream) {
+  if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  int rc = h->wait_previous();
+  if (rc) return rc;
+  if (stream) {
+    h->stream = static_cast<cudaStream_t>(stream);
+    return CLUE_OK;
+  }
+  if (!h->owned_stream) {
+    e = cudaStreamCreateWithFlags(&h->owned_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      h->owned_stream = nullptr;
+      return cuda_error(e, "cudaStreamCreate");
+    }
+  }
+  h->stream = h->owned_stream;
   return CLUE_OK;
 }
 

@@ -71,7 +71,7 @@ struct Handle {
   int device = 0;
   size_t budget = 0;
   cudaStream_t stream = nullptr;
-  bool own_stream = false;
+  cudaStream_t owned_stream = nullptr;  // created by the handle, destroyed with it
   cudaEvent_t done_event = nullptr;
   bool pending = false;
   int error_layers = kLayers;
@@ -79,6 +79,7 @@ struct Handle {
   Tuning2D tuning{};
   DeviceArena arena;
   DeviceArena arena3d;
+  DeviceArena arena_bridge;
   PinnedBuf stage;
   PinnedBuf flags_host;
   PinnedBuf nt_host;

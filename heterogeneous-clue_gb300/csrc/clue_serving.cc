@@ -102,24 +102,48 @@ class Server {
 
   int submit(int32_t n, const float* x, const float* y, const int32_t* layer, const float* w,
              const clue_outputs* out, int64_t* id) {
-    if (n < 0 || !out || !id || (n > 0 && (!x || !y || !layer || !w))) return set_error(CLUE_EINVAL, "bad argument");
-    if (n > cap_points_)
-      return set_error(CLUE_ENOMEM, "event of %d points exceeds one in-flight batch (%lld points)", n,
-                       (long long)cap_points_);
-    Request* r = new Request();
-    r->n = n;
-    r->x.assign(x, x + n);
-    r->y.assign(y, y + n);
-    r->w.assign(w, w + n);
-    r->layer.assign(layer, layer + n);
-    r->out = *out;
-    r->t_submit = Clock::now();
+    const int64_t off[2] = {0, n};
+    if (n < 0) return set_error(CLUE_EINVAL, "bad argument");
+    return submit_many(1, off, x, y, layer, w, out, id);
+  }
+
+  // Events enter the queue together, under one lock, so that the scheduler
+  // can put them in one batch.
+  int submit_many(int32_t E, const int64_t* off, const float* x, const float* y, const int32_t* layer,
+                  const float* w, const clue_outputs* outs, int64_t* ids) {
+    if (E < 0 || !outs || !ids || (E > 0 && (!off || off[0] != 0))) return set_error(CLUE_EINVAL, "bad argument");
+    for (int32_t e = 0; e < E; ++e) {
+      const int64_t n = off[e + 1] - off[e];
+      if (n < 0 || n > INT32_MAX) return set_error(CLUE_EINVAL, "bad event_offsets");
+      if (n > 0 && (!x || !y || !layer || !w)) return set_error(CLUE_EINVAL, "bad argument");
+      if (n > cap_points_)
+        return set_error(CLUE_ENOMEM, "event of %lld points exceeds one in-flight batch (%lld points)",
+                         (long long)n, (long long)cap_points_);
+    }
+    std::vector<Request*> rs(E);
+    const auto now = Clock::now();
+    for (int32_t e = 0; e < E; ++e) {
+      const int64_t s0 = off[e], n = off[e + 1] - s0;
+      Request* r = new Request();
+      r->n = (int32_t)n;
+      if (n > 0) {
+        r->x.assign(x + s0, x + s0 + n);
+        r->y.assign(y + s0, y + s0 + n);
+        r->w.assign(w + s0, w + s0 + n);
+        r->layer.assign(layer + s0, layer + s0 + n);
+      }
+      r->out = outs[e];
+      r->t_submit = now;
+      rs[e] = r;
+    }
     {
       std::lock_guard<std::mutex> g(mu_);
-      r->id = next_id_++;
-      reqs_[r->id] = r;
-      queue_.push_back(r);
-      *id = r->id;
+      for (int32_t e = 0; e < E; ++e) {
+        rs[e]->id = next_id_++;
+        reqs_[rs[e]->id] = rs[e];
+        queue_.push_back(rs[e]);
+        ids[e] = rs[e]->id;
+      }
     }
     cv_.notify_all();
     return CLUE_OK;
@@ -372,6 +396,13 @@ int clue_server_submit(clue_server* s, int32_t n, const float* x, const float* y
                        const float* weight, const clue_outputs* out, int64_t* request_id) {
   if (!s) return set_error(CLUE_EINVAL, "NULL server");
   return reinterpret_cast<Server*>(s)->submit(n, x, y, layer, weight, out, request_id);
+}
+
+int clue_server_submit_many(clue_server* s, int32_t n_events, const int64_t* event_offsets, const float* x,
+                            const float* y, const int32_t* layer, const float* weight, const clue_outputs* outs,
+                            int64_t* request_ids) {
+  if (!s) return set_error(CLUE_EINVAL, "NULL server");
+  return reinterpret_cast<Server*>(s)->submit_many(n_events, event_offsets, x, y, layer, weight, outs, request_ids);
 }
 
 int clue_server_poll(clue_server* s, int64_t id, int32_t timeout_ms, double* latency_ms) {

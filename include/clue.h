@@ -79,6 +79,12 @@ int clue_create(const clue_params* params, size_t device_budget_bytes, int devic
 int clue_destroy(clue_handle* h);
 int clue_set_params(clue_handle* h, const clue_params* params);
 
+/* Moves later work of the handle to cuda_stream (NULL: back to a stream the
+ * handle owns), after waiting for the handle's previous run.  Mirrors the
+ * per-call stream argument of CLUEAlgoCUDA::makeClusters
+ * (src/cuda/plugin-CLUEClusterizer/CLUEAlgoCUDA.h:21). */
+int clue_set_stream(clue_handle* h, void* cuda_stream);
+
 /* One event: replaces CLUEAlgoSerial::makeClusters
  * (src/serial/plugin-CLUEClusterizer/CLUEAlgoSerial.cc:18-35) and
  * CLUEAlgoCUDA::makeClusters (src/cuda/plugin-CLUEClusterizer/CLUEAlgoCUDA.cu:59-81). */
@@ -204,6 +210,51 @@ int clue3d_run_batch(clue_handle* h, const clue3d_params* params, int32_t n_even
                      const clue3d_inputs* in, const clue3d_outputs* out, int32_t* n_tracksters, int flags);
 
 /* ------------------------------------------------------------------------ */
+/* 2D -> 3D bridge: layer clusters of a clustered 2D batch, on the device.   */
+/* No reference counterpart (the reference's CLUE3D reads raw3D files,       */
+/* src/serial/bin/Source.cc:43-60).  Layer cluster c of event e is the set   */
+/* of 2D points with clusterIndex c; energy = sum of weights (exact          */
+/* fixed-point sums, so deterministic), x, y = weight-weighted means,        */
+/* layer = the seed's, z = layer_z[layer], r_over_absz = r/|z|,              */
+/* eta = asinh(z/r), phi = atan2(y, x).  Arrays are DEVICE memory;           */
+/* event_offsets, cluster_offsets and layer_z are HOST memory.  Both calls   */
+/* return when their work has finished.                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct clue_bridge_params {
+  int32_t n_layers;     /* entries of layer_z; a cluster's layer must be below it */
+  const float* layer_z; /* z (cm) of each layer */
+  float radius;         /* radius given to every layer cluster (cm) */
+  int32_t isSilicon;    /* isSilicon given to every layer cluster */
+} clue_bridge_params;
+
+typedef struct clue_layer_clusters {
+  float* x;
+  float* y;
+  float* z;
+  float* eta;
+  float* phi;
+  float* r_over_absz;
+  float* radius;
+  int32_t* layer;
+  float* energy;
+  int32_t* isSilicon;
+} clue_layer_clusters;
+
+/* Layer clusters per event (the 2D seeds) as CSR offsets: cluster_offsets
+ * (host, n_events + 1 entries) is written. */
+int clue_bridge_count(clue_handle* h, int32_t n_events, const int64_t* event_offsets, const int32_t* isSeed,
+                      int64_t* cluster_offsets);
+
+/* Builds the layer clusters (out holds cluster_offsets[n_events] entries per
+ * array, in event order, then cluster id order); the result is a CLUE3D
+ * input for clue3d_run_batch with cluster_offsets as its event offsets. */
+int clue_bridge_build(clue_handle* h, const clue_bridge_params* p, int32_t n_events, const int64_t* event_offsets,
+                      const float* x, const float* y, const int32_t* layer, const float* weight,
+                      const int32_t* isSeed, const int32_t* clusterIndex, const int64_t* cluster_offsets,
+                      const clue_layer_clusters* out);
+
+/* ------------------------------------------------------------------------ */
 /* Serving: continuous batching of CLUE 2D events                            */
 /* ------------------------------------------------------------------------ */
 
@@ -235,6 +286,14 @@ int clue_server_destroy(clue_server* s);
  * share of the budget. */
 int clue_server_submit(clue_server* s, int32_t n, const float* x, const float* y, const int32_t* layer,
                        const float* weight, const clue_outputs* out, int64_t* request_id);
+
+/* Queues n_events events at once (CSR event_offsets, host, over host x, y,
+ * layer, weight; outs holds one clue_outputs per event; request_ids receives
+ * n_events ids).  They enter the queue together, so they can share a batch.
+ * Nothing is queued when an argument is rejected. */
+int clue_server_submit_many(clue_server* s, int32_t n_events, const int64_t* event_offsets, const float* x,
+                            const float* y, const int32_t* layer, const float* weight, const clue_outputs* outs,
+                            int64_t* request_ids);
 
 /* CLUE_OK when the request's outputs are written, CLUE_EBUSY while it is
  * pending (timeout_ms = 0), CLUE_ETIMEOUT when timeout_ms ran out; <0 waits

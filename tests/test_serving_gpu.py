@@ -67,7 +67,10 @@ def test_results_identical_alone_and_in_the_mix(events, alone):
 
 def test_burst_overlaps_batches_on_device(events, alone):
     srv = C.Server(*PRM, budget_bytes=8 << 30, max_inflight=2, max_batch_events=4)
-    reqs = [srv.submit(**e) for e in events]
+    # one bulk submit: the scheduler sees the whole burst at once
+    off = np.concatenate([[0], np.cumsum([e["x"].size for e in events])]).astype(np.int64)
+    cat = {k: np.concatenate([e[k] for e in events]) for k in ("x", "y", "layer", "weight")}
+    reqs = srv.submit_many(off, cat["x"], cat["y"], cat["layer"], cat["weight"])
     srv.drain(timeout_ms=60000)
     for k, (rid, out) in enumerate(reqs):
         st, _ = srv.poll(rid, timeout_ms=0)
