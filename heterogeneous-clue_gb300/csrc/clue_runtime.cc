@@ -154,6 +154,10 @@ size_t required_bytes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bool h
 Handle::~Handle() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (done_event) cudaEventDestroy(done_event);
+  for (auto ev : pipe_events)
+    if (ev) cudaEventDestroy(ev);
+  if (copy_in) cudaStreamDestroy(copy_in);
+  if (copy_out) cudaStreamDestroy(copy_out);
   arena.release();
   if (owned_stream) cudaStreamDestroy(owned_stream);
 }
@@ -235,8 +239,10 @@ int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t*
   return CLUE_OK;
 }
 
-void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, Batch2D& b) {
-  auto P = [&](int slot) { return h->arena.ptr(slot); };
+void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, Batch2D& b,
+                      const DeviceArena* arena = nullptr) {
+  const DeviceArena& A = arena ? *arena : h->arena;
+  auto P = [&](int slot) { return A.ptr(slot); };
   b.n_events = r.E;
   b.n_points = r.N;
   b.n_chunks = (int32_t)nchunks;
@@ -315,7 +321,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
                  {(const void*)r.x, (const void*)r.y, (const void*)r.layer, (const void*)r.w,
                   (const void*)r.out->rho, (const void*)r.out->delta, (const void*)r.out->nearestHigher,
                   (const void*)r.out->isSeed, (const void*)r.out->clusterIndex, h->arena.ptr(S_OFF),
-                  h->arena.ptr(S_GX), h->arena.ptr(S_SP0), h->stage.p}};
+                  h->arena.ptr(S_GX), h->arena.ptr(S_SP0), h->stage.p, h->flags_host.p}};
     if (!h->graph_exec || !(key == h->graph_key)) {
       if (h->graph_exec) {
         cudaGraphExecDestroy(h->graph_exec);
@@ -464,6 +470,130 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   return CLUE_OK;
 }
 
+// Host-memory batches of at least 2 * kPipePoints points: the events are cut
+// into sub-batches of about kPipePoints points that alternate between two
+// device slots.  Three streams overlap the H2D copy of one sub-batch, the
+// kernels of the previous one and the D2H copy of the one before that:
+//   in-copy  : wait comp[k] (slot inputs free)  -> offsets, chunk table, x, y, layer, w -> h2d[k]
+//   compute  : wait h2d[k], d2h[k] (slot outputs free) -> kernels -> comp[k]
+//   out-copy : wait comp[k] -> rho, delta, nh, isSeed, clusterIndex, status -> d2h[k]
+// Sub-batches hold whole events, so every output is the one of the
+// unsplit batch.
+constexpr int64_t kPipePoints = int64_t(16) << 20;
+
+int run_2d_pipelined(Handle* h, const Run2D& r) {
+  int rc = h->wait_previous();
+  if (rc) return rc;
+  // event-aligned cuts
+  std::vector<int32_t> cut{0};
+  for (int32_t e = 0; e < r.E; ++e)
+    if (r.off[e + 1] - r.off[cut.back()] >= kPipePoints && e + 1 < r.E) cut.push_back(e + 1);
+  cut.push_back(r.E);
+  const int S = (int)cut.size() - 1;
+  int32_t maxE = 0;
+  int64_t maxN = 0, maxC = 0;
+  for (int i = 0; i < S; ++i) {
+    maxE = std::max(maxE, cut[i + 1] - cut[i]);
+    maxN = std::max(maxN, r.off[cut[i + 1]] - r.off[cut[i]]);
+    maxC = std::max(maxC, n_chunks_of(cut[i + 1] - cut[i], r.off + cut[i]));
+  }
+  const int grid = layer_grid_max(h->tuning, std::max(1, maxE * kLayers));
+  const auto need = sizes_2d(maxE, maxN, maxC, grid, true);
+  DeviceArena* slot_arena[2] = {&h->arena, &h->arena_pipe};
+  if ((rc = h->arena.reserve(need, h->budget))) return rc;
+  {
+    const size_t used = h->arena.total() + h->arena3d.total() + h->arena_bridge.total();
+    if ((rc = h->arena_pipe.reserve(need, h->budget > used ? h->budget - used : 0))) return rc;
+  }
+  // pinned staging: per sub-batch its rebased offsets and chunk table
+  std::vector<size_t> st_off(S + 1, 0);
+  for (int i = 0; i < S; ++i) st_off[i + 1] = st_off[i] + 16 * (size_t)(cut[i + 1] - cut[i] + 1);
+  if ((rc = h->stage.reserve(st_off[S]))) return rc;
+  if ((rc = h->flags_host.reserve(4 * kFlagCount * (size_t)S))) return rc;
+  cudaError_t e;
+  for (auto* st : {&h->copy_in, &h->copy_out}) {
+    if (!*st && (e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking)) != cudaSuccess) {
+      *st = nullptr;
+      return cuda_error(e, "cudaStreamCreate");
+    }
+  }
+  for (auto& ev : h->pipe_events) {
+    if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      ev = nullptr;
+      return cuda_error(e, "cudaEventCreate");
+    }
+  }
+  cudaEvent_t* h2d = h->pipe_events;
+  cudaEvent_t* comp = h->pipe_events + 2;
+  cudaEvent_t* d2h = h->pipe_events + 4;
+  // the in-copy stream must not overtake work queued earlier on the handle's stream
+  if ((e = cudaEventRecord(comp[0], h->stream)) != cudaSuccess ||
+      (e = cudaEventRecord(comp[1], h->stream)) != cudaSuccess ||
+      (e = cudaEventRecord(d2h[0], h->stream)) != cudaSuccess ||
+      (e = cudaEventRecord(d2h[1], h->stream)) != cudaSuccess)
+    return cuda_error(e, "cudaEventRecord");
+  int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
+  for (int i = 0; i < S; ++i) {
+    const int k = i & 1;
+    const int32_t e0 = cut[i], Es = cut[i + 1] - e0;
+    const int64_t p0 = r.off[e0], Ns = r.off[cut[i + 1]] - p0;
+    // staging: rebased offsets, then the chunk table
+    int64_t* so = reinterpret_cast<int64_t*>(static_cast<char*>(h->stage.p) + st_off[i]);
+    int32_t* sc = reinterpret_cast<int32_t*>(so + (Es + 1));
+    sc[0] = 0;
+    for (int32_t j = 0; j <= Es; ++j) so[j] = r.off[e0 + j] - p0;
+    for (int32_t j = 0; j < Es; ++j) sc[j + 1] = sc[j] + (int32_t)((so[j + 1] - so[j] + kChunk - 1) / kChunk);
+    Run2D sub = r;
+    sub.E = Es;
+    sub.N = Ns;
+    sub.off = so;
+    Batch2D b;
+    fill_batch_views(h, sub, sc[Es], true, b, slot_arena[k]);
+    const size_t n4 = 4 * (size_t)Ns;
+    cudaStream_t ci = h->copy_in, co = h->copy_out, cs = h->stream;
+    if ((e = cudaStreamWaitEvent(ci, comp[k], 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.offsets, so, 8 * (size_t)(Es + 1), cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.chunk_start, sc, 4 * (size_t)(Es + 1), cudaMemcpyHostToDevice, ci)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.x, r.x + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.y, r.y + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.layer, r.layer + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.w, r.w + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaEventRecord(h2d[k], ci)) != cudaSuccess)
+      return cuda_error(e, "H2D sub-batch");
+    if ((e = cudaStreamWaitEvent(cs, h2d[k], 0)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(cs, d2h[k], 0)) != cudaSuccess ||
+        (e = cudaMemsetAsync(b.flags + kFlagError, 0, 4, cs)) != cudaSuccess)
+      return cuda_error(e, "sub-batch set-up");
+    if ((e = launch_clue2d(b, h->p2d, h->tuning, cs)) != cudaSuccess) return cuda_error(e, "launching CLUE kernels");
+    if ((e = cudaEventRecord(comp[k], cs)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
+    const clue_outputs* o = r.out;
+    if ((e = cudaStreamWaitEvent(co, comp[k], 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->rho + p0, b.rho, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->delta + p0, b.delta, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->nearestHigher + p0, b.nh, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->isSeed + p0, b.seed, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->clusterIndex + p0, b.ci, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(fh + kFlagCount * (size_t)i, b.flags, 4 * kFlagCount, cudaMemcpyDeviceToHost, co)) !=
+            cudaSuccess ||
+        (e = cudaEventRecord(d2h[k], co)) != cudaSuccess)
+      return cuda_error(e, "D2H sub-batch");
+  }
+  // the handle's stream orders after the last copy-out, so later work and
+  // clue_synchronize see a finished batch
+  if ((e = cudaStreamWaitEvent(h->stream, d2h[(S - 1) & 1], 0)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(h->stream, d2h[S & 1], 0)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(h->copy_out)) != cudaSuccess || (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+    return cuda_error(e, "pipelined batch");
+  int err = 0;
+  for (int i = 0; i < S; ++i) {
+    err |= fh[kFlagCount * (size_t)i + kFlagError];
+    fh[kFlagCount * (size_t)i + kFlagError] = 0;
+  }
+  if (err) return set_error(CLUE_EINVAL, "a point has a layer outside [0, %d)", kLayers);
+  return CLUE_OK;
+}
+
 int run_2d(Handle* h, const Run2D& r) {
   if (r.N == 0) return CLUE_OK;
   if (!r.x || !r.y || !r.layer || !r.w || !r.out || !r.out->rho || !r.out->delta || !r.out->nearestHigher ||
@@ -472,6 +602,8 @@ int run_2d(Handle* h, const Run2D& r) {
   cudaError_t e = cudaSetDevice(h->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   if (r.flags & CLUE_PLAIN) return run_2d_plain(h, r);
+  if (!(r.flags & (CLUE_DEVICE_MEMORY | CLUE_NO_PIPELINE | kAsyncHostIO)) && r.N >= 2 * kPipePoints && r.E >= 2)
+    return run_2d_pipelined(h, r);
   return run_2d_batched(h, r);
 }
 

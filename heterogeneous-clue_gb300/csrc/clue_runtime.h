@@ -49,13 +49,13 @@ struct GraphKey {
   int threads = 0, cap = 0, ctas = 0, big_threads = 0, big_cap = 0;
   float work_tile = 0.f;
   float dc = 0.f, rhoc = 0.f, odf = 0.f;
-  const void* ptrs[13] = {};
+  const void* ptrs[14] = {};
   bool operator==(const GraphKey& o) const {
     if (E != o.E || N != o.N || flags != o.flags || threads != o.threads || cap != o.cap || ctas != o.ctas ||
         big_threads != o.big_threads || big_cap != o.big_cap ||
         work_tile != o.work_tile || dc != o.dc || rhoc != o.rhoc || odf != o.odf)
       return false;
-    for (int i = 0; i < 13; ++i)
+    for (int i = 0; i < 14; ++i)
       if (ptrs[i] != o.ptrs[i]) return false;
     return true;
   }
@@ -80,6 +80,10 @@ struct Handle {
   DeviceArena arena;
   DeviceArena arena3d;
   DeviceArena arena_bridge;
+  DeviceArena arena_pipe;                 // second slot of the pipelined host-memory path
+  cudaStream_t copy_in = nullptr;         // pipelined host-memory path: H2D stream
+  cudaStream_t copy_out = nullptr;        // and D2H stream
+  cudaEvent_t pipe_events[6] = {};        // per slot: H2D done, kernels done, D2H done
   PinnedBuf stage;
   PinnedBuf flags_host;
   PinnedBuf nt_host;

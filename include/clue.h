@@ -38,6 +38,7 @@ typedef enum clue_status {
 #define CLUE_DEVICE_MEMORY 1 /* pointers are device memory; work is queued on the handle's stream */
 #define CLUE_PLAIN 2         /* run events one at a time (the per-event launch sequence) */
 #define CLUE_NO_GRAPH 4      /* launch the batched pipeline directly instead of replaying a CUDA graph */
+#define CLUE_NO_PIPELINE 8   /* host memory: one H2D, kernels, D2H sequence instead of overlapped sub-batches */
 
 /* Parameters (src/serial/DataFormats/CLUE_config.h:8-13, without produceOutput). */
 typedef struct clue_params {

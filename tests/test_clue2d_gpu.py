@@ -237,3 +237,28 @@ def test_full_size_batch_properties(algo, torch_cuda):
         ev = S.event_of(b, e)
         want = oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *PRM)
         assert_bitexact({k: v[s:t] for k, v in got.items()}, want, label=f"event {e}")
+
+
+def test_host_memory_pipelined_large_batch(algo):
+    """Host-memory batches of at least 32M points run as overlapped
+    sub-batches (H2D, kernels and D2H on three streams over two device slots):
+    bit-identical to the single H2D-kernels-D2H sequence and, on sampled
+    events, to the oracle."""
+    b = S.uneven_batch(760, seed=29, lo=30000, hi=70000)
+    n = int(b["offsets"][-1])
+    assert n >= 32 << 20
+    got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
+    ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
+    assert_bitexact(got, ref)
+    for e in (0, 359, 759):
+        s, t = b["offsets"][e], b["offsets"][e + 1]
+        want = oracle.clue2d(b["x"][s:t], b["y"][s:t], b["layer"][s:t], b["weight"][s:t], *PRM)
+        assert_bitexact({k: v[s:t] for k, v in got.items()}, want, label=f"event {e}")
+    # an invalid layer in a late sub-batch is reported, and the handle recovers
+    bad = b["layer"].copy()
+    bad[n - 5] = 100
+    with pytest.raises(C.ClueError, match="layer"):
+        algo.run_batch(b["offsets"], b["x"], b["y"], bad, b["weight"])
+    again = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
+    assert_bitexact(again, ref)
+
