@@ -479,7 +479,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
 //   out-copy : wait comp[k] -> rho, delta, nh, isSeed, clusterIndex, status -> d2h[k]
 // Sub-batches hold whole events, so every output is the one of the
 // unsplit batch.
-constexpr int64_t kPipePoints = int64_t(16) << 20;
+constexpr int64_t kPipePoints = int64_t(8) << 20;
 
 int run_2d_pipelined(Handle* h, const Run2D& r) {
   int rc = h->wait_previous();
@@ -550,6 +550,8 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
     Batch2D b;
     fill_batch_views(h, sub, sc[Es], true, b, slot_arena[k]);
     const size_t n4 = 4 * (size_t)Ns;
+    // kernels of both slots stay on the handle's stream: letting the next
+    // sub-batch's persistent kernel start beside the draining one measured slower
     cudaStream_t ci = h->copy_in, co = h->copy_out, cs = h->stream;
     if ((e = cudaStreamWaitEvent(ci, comp[k], 0)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.offsets, so, 8 * (size_t)(Es + 1), cudaMemcpyHostToDevice, ci)) != cudaSuccess ||

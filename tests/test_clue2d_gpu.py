@@ -240,13 +240,13 @@ def test_full_size_batch_properties(algo, torch_cuda):
 
 
 def test_host_memory_pipelined_large_batch(algo):
-    """Host-memory batches of at least 32M points run as overlapped
+    """Host-memory batches of at least 16M points run as overlapped
     sub-batches (H2D, kernels and D2H on three streams over two device slots):
     bit-identical to the single H2D-kernels-D2H sequence and, on sampled
     events, to the oracle."""
     b = S.uneven_batch(760, seed=29, lo=30000, hi=70000)
     n = int(b["offsets"][-1])
-    assert n >= 32 << 20
+    assert n >= 32 << 20  # four or more sub-batches
     got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
     assert_bitexact(got, ref)
