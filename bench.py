@@ -190,41 +190,52 @@ def serving_leg(C, b, rate, n_req, batched=True):
     """Poisson arrivals of events from the workload at ``rate`` events/s into
     the continuous-batching server (batched) or into a one-event-per-launch
     server (plain: one batch of one event in flight); latency is submit ->
-    outputs written, measured by the server."""
+    outputs written, measured by the server.  Requests are consecutive events
+    of the workload; the client submits every request whose arrival time has
+    passed in one bulk call (``submit_many``), so that the offered load is not
+    capped by the submitting thread."""
     import numpy as np
 
-    from clue_gb300 import synthetic as S
     E = b["offsets"].size - 1
+    off = b["offsets"]
     rng = np.random.default_rng(5)
-    idx = rng.integers(0, E, n_req)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
-    views = [S.event_of(b, int(e)) for e in idx]
     srv = C.Server(*PARAMS, budget_bytes=16 << 30, max_inflight=2 if batched else 1,
                    max_batch_events=256 if batched else 1)
+
+    def submit(i, j):  # requests i..j-1 = events i % E .. (j - 1) % E, no wrap inside
+        e0 = i % E
+        s, t = off[e0], off[e0 + (j - i)]
+        sub = off[e0:e0 + (j - i) + 1] - s
+        return srv.submit_many(sub, b["x"][s:t], b["y"][s:t], b["layer"][s:t], b["weight"][s:t])
+
     # warm the slots (allocation, first launches) outside the measurement
-    warm = [srv.submit(**views[i]) for i in range(min(8, n_req))]
+    warm = submit(0, min(8, n_req))
     srv.drain()
     for rid, _ in warm:
         srv.poll(rid, 0)
     srv.reset_stats()
     t0 = time.perf_counter()
     ids = []
-    for i in range(n_req):
-        target = t0 + arrivals[i]
-        while True:
-            now = time.perf_counter()
-            if now >= target:
-                break
-            if target - now > 0.002:
-                time.sleep(target - now - 0.001)
-        ids.append(srv.submit(**views[i]))
+    i = 0
+    while i < n_req:
+        now = time.perf_counter() - t0
+        j = int(np.searchsorted(arrivals, now, side="right"))
+        if j > i:
+            j = min(j, i + (E - i % E))  # a burst never wraps around the workload
+            ids += submit(i, j)
+            i = j
+            continue
+        wait = arrivals[i] - now
+        if wait > 0.002:
+            time.sleep(wait - 0.001)
     srv.drain()
     elapsed = time.perf_counter() - t0
     st = srv.stats()
     for rid, _ in ids:
         srv.poll(rid, 0)
     srv.close()
-    pts = sum(int(v["x"].size) for v in views)
+    pts = int(sum(int(off[(k % E) + 1] - off[k % E]) for k in range(n_req)))
     return {"offered_events_per_s": rate, "requests": n_req, "achieved_events_per_s": n_req / elapsed,
             "achieved_gpoints_per_s": pts / elapsed / 1e9, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
             "mean_batch_events": st["mean_batch_events"], "max_inflight_seen": st["max_inflight_seen"],
@@ -390,6 +401,12 @@ def run_gb300(args):
         serving = {"batched": serving_leg(C, b, args.serving_rate, args.serving_requests, batched=True),
                    "plain": serving_leg(C, b, args.serving_rate, max(200, args.serving_requests // 4),
                                         batched=False)}
+        if args.serving_high_rate > 0:
+            # above the one-event server's capacity: batches form, the plain queue grows
+            serving["high_load"] = {
+                "batched": serving_leg(C, b, args.serving_high_rate, args.serving_requests, batched=True),
+                "plain": serving_leg(C, b, args.serving_high_rate, max(200, args.serving_requests // 4),
+                                     batched=False)}
     clue3d = None
     if rank == 0 and not args.no_clue3d:
         clue3d = clue3d_leg(C, torch, stream, args)
@@ -436,6 +453,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-rate", type=float, default=2000.0)
+    ap.add_argument("--serving-high-rate", type=float, default=20000.0,
+                    help="second offered load (events/s) above the plain server's capacity; 0 = skip")
     ap.add_argument("--serving-requests", type=int, default=3000)
     ap.add_argument("--no-clue3d", action="store_true")
     ap.add_argument("--clue3d-events", type=int, default=1000)

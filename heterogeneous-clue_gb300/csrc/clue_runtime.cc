@@ -52,11 +52,23 @@ void DeviceArena::release() {
   total_ = 0;
 }
 
-int DeviceArena::reserve(const std::vector<size_t>& need, size_t budget) {
-  size_t want = 0;
-  for (size_t i = 0; i < need.size(); ++i) want += std::max(need[i], i < bufs_.size() ? bufs_[i].bytes : 0);
+int DeviceArena::reserve(const std::vector<size_t>& need_in, size_t budget) {
+  // A buffer that must grow grows by at least half its size when the budget
+  // allows, so that slowly rising request sizes do not reallocate every call.
+  std::vector<size_t> need = need_in;
+  size_t want = 0, want_grown = 0;
+  for (size_t i = 0; i < need.size(); ++i) {
+    const size_t have = i < bufs_.size() ? bufs_[i].bytes : 0;
+    want += std::max(need[i], have);
+    want_grown += need[i] <= have ? have : std::max(need[i], have + have / 2);
+  }
   if (want > budget)
     return set_error(CLUE_ENOMEM, "request needs %zu device bytes, budget is %zu", want, budget);
+  if (want_grown <= budget)
+    for (size_t i = 0; i < need.size(); ++i) {
+      const size_t have = i < bufs_.size() ? bufs_[i].bytes : 0;
+      if (need[i] > have) need[i] = std::max(need[i], have + have / 2);
+    }
   if (bufs_.size() < need.size()) bufs_.resize(need.size());
   for (size_t i = 0; i < need.size(); ++i) {
     if (need[i] <= bufs_[i].bytes) continue;
@@ -85,10 +97,10 @@ PinnedBuf::~PinnedBuf() {
 
 int PinnedBuf::reserve(size_t n) {
   if (n <= bytes) return CLUE_OK;
+  const size_t b = std::max<size_t>({n, size_t(4096), bytes + bytes / 2});
   if (p) cudaFreeHost(p);
   p = nullptr;
   bytes = 0;
-  size_t b = std::max<size_t>(n, 4096);
   cudaError_t e = cudaHostAlloc(&p, b, cudaHostAllocDefault);
   if (e != cudaSuccess) return cuda_error(e, "cudaHostAlloc");
   bytes = b;
@@ -149,6 +161,15 @@ size_t required_bytes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bool h
   size_t t = 0;
   for (size_t v : s) t += (v + 255) & ~size_t(255);
   return t;
+}
+
+int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io) {
+  const int64_t nchunks = N / kChunk + E;
+  const int grid = layer_grid_max(h->tuning, std::max(1, E * kLayers));
+  int rc = h->arena.reserve(sizes_2d(E, N, nchunks, grid, host_io), h->budget);
+  if (!rc) rc = h->stage.reserve(24 * (size_t)(E + 1));
+  if (!rc) rc = h->flags_host.reserve(4 * kFlagCount);
+  return rc;
 }
 
 Handle::~Handle() {

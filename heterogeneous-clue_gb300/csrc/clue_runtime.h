@@ -62,6 +62,11 @@ struct GraphKey {
 };
 
 size_t required_bytes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bool host_io);
+struct Handle;
+// Sizes the handle's 2D buffers for a batch of E events and N points ahead of
+// time (a server slot does this at start so that its first batches do not
+// allocate).
+int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io);
 
 // Internal run flag: host (pinned) buffers, but return once the work is
 // queued; completion is seen through Handle::done_event.  Used by the server.

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -33,6 +34,40 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Host copies of the serving path (request staging and result delivery).
+// Large sets are cut into 1 MB pieces and spread over a few threads.
+struct CopyTask {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
+void run_copies(const std::vector<CopyTask>& tasks) {
+  constexpr size_t kPiece = size_t(1) << 20;
+  size_t total = 0;
+  for (const auto& t : tasks) total += t.bytes;
+  const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
+  const size_t nth = std::min<size_t>({size_t(8), size_t(hw / 2), total / (4 * kPiece)});
+  if (nth <= 1) {
+    for (const auto& t : tasks)
+      if (t.bytes) memcpy(t.dst, t.src, t.bytes);
+    return;
+  }
+  std::vector<CopyTask> pieces;
+  for (const auto& t : tasks)
+    for (size_t o = 0; o < t.bytes; o += kPiece)
+      pieces.push_back({static_cast<char*>(t.dst) + o, static_cast<const char*>(t.src) + o,
+                        std::min(kPiece, t.bytes - o)});
+  std::atomic<size_t> next{0};
+  auto work = [&] {
+    for (size_t i; (i = next.fetch_add(1)) < pieces.size();) memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+  };
+  std::vector<std::thread> th;
+  for (size_t k = 1; k < nth; ++k) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+}
+
 struct Request {
   int64_t id = 0;
   int32_t n = 0;
@@ -49,7 +84,8 @@ struct Slot {
   PinnedBuf in, out;
   std::vector<int64_t> off;
   std::vector<Request*> reqs;
-  bool busy = false;
+  bool busy = false;      // requests taken (staging, on the device or delivering results)
+  bool launched = false;  // the batch is queued on the device
   int64_t cap_points = 0;
 };
 
@@ -78,6 +114,14 @@ class Server {
       }
       s.cap_points = lo;
       if (s.cap_points < 1) return set_error(CLUE_ENOMEM, "budget too small for one in-flight batch");
+      // resident buffers for batches up to 8M points, so that ordinary loads
+      // never allocate (and never synchronise the device) on the serving path
+      const int64_t pre = std::min<int64_t>(s.cap_points, int64_t(8) << 20);
+      cudaSetDevice(cfg_.device);
+      rc = reserve_2d(hh, cfg_.max_batch_events, pre, true);
+      if (!rc) rc = s.in.reserve(16 * (size_t)pre);
+      if (!rc) rc = s.out.reserve(20 * (size_t)pre);
+      if (rc) return rc;
     }
     cap_points_ = slots_[0].cap_points;
     worker_ = std::thread([this] { loop(); });
@@ -122,20 +166,27 @@ class Server {
     }
     std::vector<Request*> rs(E);
     const auto now = Clock::now();
+    std::vector<CopyTask> copies;
+    copies.reserve(4 * (size_t)E);
     for (int32_t e = 0; e < E; ++e) {
       const int64_t s0 = off[e], n = off[e + 1] - s0;
       Request* r = new Request();
       r->n = (int32_t)n;
       if (n > 0) {
-        r->x.assign(x + s0, x + s0 + n);
-        r->y.assign(y + s0, y + s0 + n);
-        r->w.assign(w + s0, w + s0 + n);
-        r->layer.assign(layer + s0, layer + s0 + n);
+        r->x.resize(n);
+        r->y.resize(n);
+        r->w.resize(n);
+        r->layer.resize(n);
+        copies.push_back({r->x.data(), x + s0, 4 * (size_t)n});
+        copies.push_back({r->y.data(), y + s0, 4 * (size_t)n});
+        copies.push_back({r->w.data(), w + s0, 4 * (size_t)n});
+        copies.push_back({r->layer.data(), layer + s0, 4 * (size_t)n});
       }
       r->out = outs[e];
       r->t_submit = now;
       rs[e] = r;
     }
+    run_copies(copies);
     {
       std::lock_guard<std::mutex> g(mu_);
       for (int32_t e = 0; e < E; ++e) {
@@ -214,11 +265,14 @@ class Server {
   }
 
  private:
-  // Completes every finished slot; called with mu_ held.
-  bool reap() {
-    bool any = false;
+  // Completes every finished slot.  Called with mu_ held; the result copies
+  // run with the lock released (only this thread touches slots), and the
+  // statuses are published under the lock afterwards.
+  bool reap(std::unique_lock<std::mutex>& g) {
+    std::vector<Slot*> done;
+    std::vector<int> sts;
     for (auto& s : slots_) {
-      if (!s.busy) continue;
+      if (!s.busy || !s.launched) continue;
       Handle* h = reinterpret_cast<Handle*>(s.h);
       cudaError_t q = cudaEventQuery(h->done_event);
       if (q == cudaErrorNotReady) continue;
@@ -229,42 +283,52 @@ class Server {
         h->pending = false;
         st = h->check_device_flags();
       }
-      const auto now = Clock::now();
+      done.push_back(&s);
+      sts.push_back(st);
+    }
+    if (done.empty()) return false;
+    g.unlock();
+    std::vector<CopyTask> copies;
+    for (size_t d = 0; d < done.size(); ++d) {
+      Slot& s = *done[d];
+      if (sts[d] != CLUE_OK) continue;
       const char* ob = static_cast<const char*>(s.out.p);
       const int64_t N = s.off.back();
       for (size_t k = 0; k < s.reqs.size(); ++k) {
         Request* r = s.reqs[k];
         const int64_t o = s.off[k];
         const size_t b = 4 * (size_t)r->n;
-        if (st == CLUE_OK && r->n > 0) {
-          memcpy(r->out.rho, ob + 4 * o, b);
-          memcpy(r->out.delta, ob + 4 * (N + o), b);
-          memcpy(r->out.nearestHigher, ob + 4 * (2 * N + o), b);
-          memcpy(r->out.isSeed, ob + 4 * (3 * N + o), b);
-          memcpy(r->out.clusterIndex, ob + 4 * (4 * N + o), b);
-        }
+        if (r->n == 0) continue;
+        copies.push_back({r->out.rho, ob + 4 * o, b});
+        copies.push_back({r->out.delta, ob + 4 * (N + o), b});
+        copies.push_back({r->out.nearestHigher, ob + 4 * (2 * N + o), b});
+        copies.push_back({r->out.isSeed, ob + 4 * (3 * N + o), b});
+        copies.push_back({r->out.clusterIndex, ob + 4 * (4 * N + o), b});
+      }
+    }
+    run_copies(copies);
+    const auto now = Clock::now();
+    g.lock();
+    for (size_t d = 0; d < done.size(); ++d) {
+      Slot& s = *done[d];
+      for (Request* r : s.reqs) {
         r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
-        r->status = st;
-        if (st == CLUE_OK) lat_.push_back(r->latency_ms);
-        r->x.clear();
-        r->x.shrink_to_fit();
-        r->y.clear();
-        r->y.shrink_to_fit();
-        r->w.clear();
-        r->w.shrink_to_fit();
-        r->layer.clear();
-        r->layer.shrink_to_fit();
+        r->status = sts[d];
+        if (sts[d] == CLUE_OK) lat_.push_back(r->latency_ms);
       }
       s.reqs.clear();
       s.busy = false;
-      any = true;
+      s.launched = false;
     }
-    if (any) done_cv_.notify_all();
-    return any;
+    done_cv_.notify_all();
+    return true;
   }
 
-  // Admits queued requests into a free slot and launches it; mu_ held.
-  void admit(Slot& s) {
+  // Admits queued requests into a free slot and launches it.  Called with mu_
+  // held; the requests are taken (and the slot marked busy, so that drain()
+  // keeps waiting) under the lock, the staging copies and the launch run
+  // without it.
+  void admit(Slot& s, std::unique_lock<std::mutex>& g) {
     s.reqs.clear();
     s.off.assign(1, 0);
     int64_t pts = 0;
@@ -278,18 +342,30 @@ class Server {
     }
     const int32_t E = (int32_t)s.reqs.size();
     if (E == 0) return;
+    s.busy = true;
+    g.unlock();
     int rc = s.in.reserve(16 * (size_t)std::max<int64_t>(pts, 1));
     if (!rc) rc = s.out.reserve(20 * (size_t)std::max<int64_t>(pts, 1));
     if (!rc) {
       char* ib = static_cast<char*>(s.in.p);
+      std::vector<CopyTask> copies;
+      copies.reserve(4 * (size_t)E);
       for (int32_t k = 0; k < E; ++k) {
         Request* r = s.reqs[k];
         const int64_t o = s.off[k];
         const size_t b = 4 * (size_t)r->n;
-        memcpy(ib + 4 * o, r->x.data(), b);
-        memcpy(ib + 4 * (pts + o), r->y.data(), b);
-        memcpy(ib + 4 * (2 * pts + o), r->layer.data(), b);
-        memcpy(ib + 4 * (3 * pts + o), r->w.data(), b);
+        if (r->n == 0) continue;
+        copies.push_back({ib + 4 * o, r->x.data(), b});
+        copies.push_back({ib + 4 * (pts + o), r->y.data(), b});
+        copies.push_back({ib + 4 * (2 * pts + o), r->layer.data(), b});
+        copies.push_back({ib + 4 * (3 * pts + o), r->w.data(), b});
+      }
+      run_copies(copies);
+      for (Request* r : s.reqs) {  // inputs are staged: free them now
+        std::vector<float>().swap(r->x);
+        std::vector<float>().swap(r->y);
+        std::vector<float>().swap(r->w);
+        std::vector<int32_t>().swap(r->layer);
       }
       char* ob = static_cast<char*>(s.out.p);
       clue_outputs out{reinterpret_cast<float*>(ob), reinterpret_cast<float*>(ob + 4 * pts),
@@ -302,16 +378,18 @@ class Server {
                         reinterpret_cast<const float*>(ib + 12 * pts), &out,
                         CLUE_HOST_MEMORY | CLUE_NO_GRAPH | kAsyncHostIO);
     }
+    g.lock();
     if (rc) {
       for (Request* r : s.reqs) {
         r->status = rc;
         r->latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
       }
       s.reqs.clear();
+      s.busy = false;
       done_cv_.notify_all();
       return;
     }
-    s.busy = true;
+    s.launched = true;
     ++batches_;
     batched_events_ += E;
     int inflight = 0;
@@ -323,7 +401,7 @@ class Server {
     cudaSetDevice(cfg_.device);
     std::unique_lock<std::mutex> g(mu_);
     while (!stop_) {
-      reap();
+      reap(g);
       Slot* free_slot = nullptr;
       bool busy = false;
       for (auto& s : slots_) {
@@ -331,7 +409,7 @@ class Server {
         busy |= s.busy;
       }
       if (free_slot && !queue_.empty()) {
-        admit(*free_slot);
+        admit(*free_slot, g);
         continue;
       }
       if (busy) {
@@ -343,8 +421,8 @@ class Server {
     }
     // finish what is in flight before the slots are destroyed
     for (auto& s : slots_)
-      if (s.busy) cudaEventSynchronize(reinterpret_cast<Handle*>(s.h)->done_event);
-    reap();
+      if (s.launched) cudaEventSynchronize(reinterpret_cast<Handle*>(s.h)->done_event);
+    reap(g);
     for (Request* r : queue_) r->status = CLUE_EINVAL;
     queue_.clear();
     done_cv_.notify_all();
