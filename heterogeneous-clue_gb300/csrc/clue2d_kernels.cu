@@ -535,30 +535,56 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
 __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
   const int c = blockIdx.x;
   __shared__ int s_e;
+  __shared__ int s_cnt[kLayers];
+  for (int l = threadIdx.x; l < kLayers; l += kChunkThreads) s_cnt[l] = 0;
   if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
   __syncthreads();
   const int e = s_e;
   const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
   const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
   const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
+  const int lane = lane_id();
   bool ungrouped = false;
-  for (int64_t base = i0; base < i1; base += kChunkThreads) {
-    const int64_t i = base + threadIdx.x;
+  // all loads of the chunk first, so that they are in flight together
+  constexpr int PER = kChunk / kChunkThreads;
+  int lv[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
+    lv[j] = i < i1 ? b.layer[i] : 0;
+  }
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
     int key = -1;
+    const int l = lv[j];
     if (i < i1) {
-      const int l = b.layer[i];
       if (l < 0 || l >= kLayers) {
         atomicExch(&b.flags[kFlagError], 1);
         ungrouped = true;
       } else {
-        key = e * kLayers + l;
-        if (i > es && l < b.layer[i - 1]) ungrouped = true;
+        key = l;
       }
     }
-    const unsigned mask = __match_any_sync(0xffffffffu, key);
-    if (key >= 0 && lane_id() == __ffs(mask) - 1) atomicAdd(&b.lcnt[key], __popc(mask));
+    // grouped input: a point's layer is not below its predecessor's (the
+    // predecessor of lane 0 is read from memory, the others by shuffle)
+    const int prev = __shfl_up_sync(0xffffffffu, l, 1);
+    if (key >= 0 && i > es) {
+      const int pl = lane ? prev : b.layer[i - 1];
+      if (l < pl) ungrouped = true;
+    }
+    // most warps of grouped input hold one layer: one increment for the warp
+    const int k0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == k0)) {
+      if (lane == 0 && k0 >= 0) atomicAdd(&s_cnt[k0], 32);
+    } else {
+      const unsigned mask = __match_any_sync(0xffffffffu, key);
+      if (key >= 0 && lane == __ffs(mask) - 1) atomicAdd(&s_cnt[key], __popc(mask));
+    }
   }
   if (__syncthreads_or(ungrouped) && threadIdx.x == 0) b.flags[kFlagGrouped] = 0;
+  for (int l = threadIdx.x; l < kLayers; l += kChunkThreads)
+    if (s_cnt[l]) atomicAdd(&b.lcnt[e * kLayers + l], s_cnt[l]);
 }
 
 // One warp per event: layers 4*lane .. 4*lane+3.
@@ -776,13 +802,23 @@ __global__ void __launch_bounds__(kChunkThreads) k_label(Batch2D b) {
   const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
   const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
   const int64_t n_ev = ee - es;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += kChunkThreads) {
-    if (!b.seed[i]) {
-      // v is the event-local index of the root seed (or -1); points with an
-      // invalid layer were never written, so v is range-checked
-      const int v = b.ci[i];
-      b.ci[i] = (v >= 0 && v < n_ev) ? b.ci[es + v] : -1;
-    }
+  // v is the event-local index of the root seed (or -1); points with an
+  // invalid layer were never written, so v is range-checked.  The roots are
+  // seeds, which this kernel never writes; the gathers of one thread's points
+  // are issued together.
+  constexpr int PER = kChunk / kChunkThreads;
+  int v[PER], r[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
+    v[j] = (i < i1 && !b.seed[i]) ? b.ci[i] : INT_MIN;
+  }
+#pragma unroll
+  for (int j = 0; j < PER; ++j) r[j] = (v[j] >= 0 && v[j] < n_ev) ? b.ci[es + v[j]] : -1;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
+    if (v[j] != INT_MIN) b.ci[i] = r[j];
   }
 }
 
