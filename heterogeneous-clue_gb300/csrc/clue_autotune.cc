@@ -51,14 +51,16 @@ bool cache_lookup(const char* path, const std::string& gpu, const std::string& k
   while (std::getline(f, line)) {
     if (line.find("\"gpu\": \"" + gpu + "\"") == std::string::npos) continue;
     if (line.find("\"key\": \"" + key + "\"") == std::string::npos) continue;
+    if (line.find("\"format\": 2") == std::string::npos) continue;  // entries of older layouts are retuned
     Tuning2D c;
-    if (sscanf(strstr(line.c_str(), "\"threads\":"), "\"threads\": %d", &c.threads) != 1) continue;
-    const char* q = strstr(line.c_str(), "\"layer_capacity\":");
-    if (!q || sscanf(q, "\"layer_capacity\": %d", &c.layer_capacity) != 1) continue;
-    q = strstr(line.c_str(), "\"work_tile_cm\":");
-    if (!q || sscanf(q, "\"work_tile_cm\": %f", &c.work_tile_cm) != 1) continue;
-    q = strstr(line.c_str(), "\"ctas_per_sm\":");
-    if (!q || sscanf(q, "\"ctas_per_sm\": %d", &c.ctas_per_sm) != 1) continue;
+    auto get = [&](const char* name, int* v) {
+      const char* q = strstr(line.c_str(), name);
+      return q && sscanf(q + strlen(name), " %d", v) == 1;
+    };
+    if (!get("\"threads\":", &c.threads) || !get("\"layer_capacity\":", &c.layer_capacity) ||
+        !get("\"ctas_per_sm\":", &c.ctas_per_sm) || !get("\"big_threads\":", &c.big_threads) ||
+        !get("\"big_capacity\":", &c.big_capacity))
+      continue;
     *t = c;  // the last matching line wins
     found = true;
   }
@@ -68,9 +70,10 @@ bool cache_lookup(const char* path, const std::string& gpu, const std::string& k
 void cache_store(const char* path, const std::string& gpu, const std::string& key, const Tuning2D& t, float ms) {
   if (!path) return;
   std::ofstream f(path, std::ios::app);
-  f << "{\"gpu\": \"" << gpu << "\", \"key\": \"" << key << "\", \"threads\": " << t.threads
-    << ", \"layer_capacity\": " << t.layer_capacity << ", \"work_tile_cm\": " << t.work_tile_cm
-    << ", \"ctas_per_sm\": " << t.ctas_per_sm << ", \"ms\": " << ms << "}\n";
+  f << "{\"format\": 2, \"gpu\": \"" << gpu << "\", \"key\": \"" << key << "\", \"threads\": " << t.threads
+    << ", \"layer_capacity\": " << t.layer_capacity << ", \"ctas_per_sm\": " << t.ctas_per_sm
+    << ", \"big_threads\": " << t.big_threads << ", \"big_capacity\": " << t.big_capacity << ", \"ms\": " << ms
+    << "}\n";
 }
 
 }  // namespace
@@ -93,23 +96,25 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
   } else {
     int smem_optin = 0;
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    // Stage 1: the first pass (threads, on-chip capacity) with the handle's
+    // second pass; stage 2 (below): the second pass for the stage-1 winner.
     std::vector<Tuning2D> cands;
     const int caps[] = {1024, 1536, 2048, 2560};
     const int threads[] = {128, 256, 512};
-    const float tiles[] = {0.f};
     for (int th : threads)
-      for (int cap : caps)
-        for (float wt : tiles) {
-          Tuning2D t;
-          t.threads = th;
-          t.layer_capacity = cap;
-          t.work_tile_cm = wt;
-          t.ctas_per_sm = 0;
-          t.big_threads = h->tuning.big_threads;
-          t.big_capacity = h->tuning.big_capacity;
-          if (layer_smem_bytes(t) + 1024 > (size_t)smem_optin) continue;
-          cands.push_back(t);
-        }
+      for (int cap : caps) {
+        Tuning2D t;
+        t.threads = th;
+        t.layer_capacity = cap;
+        t.work_tile_cm = 0.f;
+        t.ctas_per_sm = 0;
+        t.big_threads = h->tuning.big_threads;
+        t.big_capacity = h->tuning.big_capacity;
+        if (layer_smem_bytes(t) + 1024 > (size_t)smem_optin) continue;
+        cands.push_back(t);
+      }
+    const size_t stage1 = cands.size();
+    const int big[][2] = {{512, 8192}, {512, 4096}, {256, 4096}, {512, 2560}, {256, 2560}, {0, 0}};
     unsigned long long* d_dig = nullptr;
     if (cudaMalloc(&d_dig, sizeof(unsigned long long)) != cudaSuccess) {
       cudaGetLastError();
@@ -123,7 +128,19 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
     float best_ms = 1e30f;
     int rc = CLUE_OK;
     const Tuning2D saved = h->tuning;
-    for (size_t ci = 0; ci < cands.size() && rc == CLUE_OK; ++ci) {
+    for (size_t ci = 0; rc == CLUE_OK; ++ci) {
+      if (ci == stage1) {  // stage 2: second-pass variants of the stage-1 winner
+        for (const auto& bp : big) {
+          Tuning2D t = best;
+          t.big_threads = bp[0];
+          t.big_capacity = bp[1];
+          if (bp[0] && t.big_capacity <= t.layer_capacity) continue;
+          if (t.big_threads == best.big_threads && t.big_capacity == best.big_capacity) continue;
+          if (bp[0] && layer_smem_bytes(Tuning2D{t.big_threads, t.big_capacity}) + 1024 > (size_t)smem_optin) continue;
+          cands.push_back(t);
+        }
+      }
+      if (ci >= cands.size()) break;
       h->tuning = cands[ci];
       const int flags = CLUE_DEVICE_MEMORY | CLUE_NO_GRAPH;
       rc = h->run_batch(E, off, x, y, layer, w, out, flags);  // warm-up (and allocation)
@@ -156,8 +173,9 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
       if (ci == 0) {
         ref_digest = dig;
       } else if (dig != ref_digest) {
-        rc = set_error(CLUE_ECUDA, "autotune: candidate (threads %d, capacity %d, tile %.2f) changed the outputs",
-                       cands[ci].threads, cands[ci].layer_capacity, cands[ci].work_tile_cm);
+        rc = set_error(CLUE_ECUDA,
+                       "autotune: candidate (threads %d, capacity %d, second pass %d x %d) changed the outputs",
+                       cands[ci].threads, cands[ci].layer_capacity, cands[ci].big_threads, cands[ci].big_capacity);
         break;
       }
       if (ms < best_ms) {
@@ -180,6 +198,8 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
     chosen->layer_capacity = best.layer_capacity;
     chosen->work_tile_cm = best.work_tile_cm;
     chosen->ctas_per_sm = best.ctas_per_sm;
+    chosen->big_threads = best.big_threads;
+    chosen->big_capacity = best.big_capacity;
   }
   return CLUE_OK;
 }

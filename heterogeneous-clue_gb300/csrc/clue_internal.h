@@ -52,7 +52,7 @@ struct Tuning2D {
   float work_tile_cm = 0.f;
   int ctas_per_sm = 0;
   int big_threads = 512;     // second pass for layers above layer_capacity (0 = none)
-  int big_capacity = 8192;
+  int big_capacity = 4096;
 };
 
 // Device views of one 2D batch.  All [N] arrays are in the caller's point order

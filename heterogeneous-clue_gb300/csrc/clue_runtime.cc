@@ -806,8 +806,7 @@ int clue_set_tuning(clue_handle* hh, const clue_tuning* t) {
     return set_error(CLUE_EINVAL, "threads must be 128, 256, 512 or 1024");
   if (t->layer_capacity < 32 || clue::layer_smem_bytes(clue::Tuning2D{t->threads, t->layer_capacity}) > 227 * 1024 - 1024)
     return set_error(CLUE_EINVAL, "layer_capacity %d does not fit in shared memory", t->layer_capacity);
-  if (!(t->work_tile_cm == 0.f || (t->work_tile_cm >= 0.5f && t->work_tile_cm <= 4.f)))
-    return set_error(CLUE_EINVAL, "work_tile_cm must be 0 or in [0.5, 4]");
+  if (t->work_tile_cm != 0.f) return set_error(CLUE_EINVAL, "work_tile_cm is reserved and must be 0");
   if (t->ctas_per_sm < 0 || t->ctas_per_sm > 8) return set_error(CLUE_EINVAL, "ctas_per_sm must be in [0, 8]");
   if (t->big_threads != 0 && t->big_threads != 128 && t->big_threads != 256 && t->big_threads != 512 &&
       t->big_threads != 1024)

@@ -62,7 +62,7 @@ typedef struct clue_outputs {
 typedef struct clue_tuning {
   int32_t threads;        /* threads per CTA of the layer kernel: 128, 256, 512 or 1024 */
   int32_t layer_capacity; /* points of one layer held on-chip; larger layers use HBM scratch */
-  float work_tile_cm;     /* query grouping inside a 5 cm tile: 0 (none) or 0.5 .. 4 cm */
+  float work_tile_cm;     /* reserved, must be 0: the 5 cm tiles are the reference's and a layer is one work unit */
   int32_t ctas_per_sm;    /* 0 = as many as shared memory allows */
   int32_t big_threads;    /* second pass for layers above layer_capacity: threads per CTA, 0 = none */
   int32_t big_capacity;   /* on-chip points of that pass; larger layers use HBM scratch */
