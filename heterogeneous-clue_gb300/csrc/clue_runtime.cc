@@ -492,8 +492,8 @@ int run_2d_plain(Handle* h, const Run2D& r) {
 }
 
 // Host-memory batches of at least 2 * kPipePoints points: the events are cut
-// into sub-batches of about kPipePoints points that alternate between two
-// device slots.  Three streams overlap the H2D copy of one sub-batch, the
+// into sub-batches of about kPipePoints points that take turns on
+// kPipeSlots device slots.  Three streams overlap the H2D copy of one sub-batch, the
 // kernels of the previous one and the D2H copy of the one before that:
 //   in-copy  : wait comp[k] (slot inputs free)  -> offsets, chunk table, x, y, layer, w -> h2d[k]
 //   compute  : wait h2d[k], d2h[k] (slot outputs free) -> kernels -> comp[k]
@@ -520,11 +520,15 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
   }
   const int grid = layer_grid_max(h->tuning, std::max(1, maxE * kLayers));
   const auto need = sizes_2d(maxE, maxN, maxC, grid, true);
-  DeviceArena* slot_arena[2] = {&h->arena, &h->arena_pipe};
+  DeviceArena* slot_arena[kPipeSlots];
+  slot_arena[0] = &h->arena;
+  for (int k = 1; k < kPipeSlots; ++k) slot_arena[k] = &h->arena_pipe[k - 1];
   if ((rc = h->arena.reserve(need, h->budget))) return rc;
-  {
-    const size_t used = h->arena.total() + h->arena3d.total() + h->arena_bridge.total();
-    if ((rc = h->arena_pipe.reserve(need, h->budget > used ? h->budget - used : 0))) return rc;
+  for (int k = 1; k < kPipeSlots; ++k) {
+    size_t used = h->arena3d.total() + h->arena_bridge.total();
+    for (int j = 0; j < kPipeSlots; ++j)
+      if (j != k) used += slot_arena[j]->total();
+    if ((rc = slot_arena[k]->reserve(need, h->budget > used ? h->budget - used : 0))) return rc;
   }
   // pinned staging: per sub-batch its rebased offsets and chunk table
   std::vector<size_t> st_off(S + 1, 0);
@@ -545,17 +549,16 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
     }
   }
   cudaEvent_t* h2d = h->pipe_events;
-  cudaEvent_t* comp = h->pipe_events + 2;
-  cudaEvent_t* d2h = h->pipe_events + 4;
+  cudaEvent_t* comp = h->pipe_events + kPipeSlots;
+  cudaEvent_t* d2h = h->pipe_events + 2 * kPipeSlots;
   // the in-copy stream must not overtake work queued earlier on the handle's stream
-  if ((e = cudaEventRecord(comp[0], h->stream)) != cudaSuccess ||
-      (e = cudaEventRecord(comp[1], h->stream)) != cudaSuccess ||
-      (e = cudaEventRecord(d2h[0], h->stream)) != cudaSuccess ||
-      (e = cudaEventRecord(d2h[1], h->stream)) != cudaSuccess)
-    return cuda_error(e, "cudaEventRecord");
+  for (int k = 0; k < kPipeSlots; ++k)
+    if ((e = cudaEventRecord(comp[k], h->stream)) != cudaSuccess ||
+        (e = cudaEventRecord(d2h[k], h->stream)) != cudaSuccess)
+      return cuda_error(e, "cudaEventRecord");
   int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
   for (int i = 0; i < S; ++i) {
-    const int k = i & 1;
+    const int k = i % kPipeSlots;
     const int32_t e0 = cut[i], Es = cut[i + 1] - e0;
     const int64_t p0 = r.off[e0], Ns = r.off[cut[i + 1]] - p0;
     // staging: rebased offsets, then the chunk table
@@ -604,9 +607,9 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
   }
   // the handle's stream orders after the last copy-out, so later work and
   // clue_synchronize see a finished batch
-  if ((e = cudaStreamWaitEvent(h->stream, d2h[(S - 1) & 1], 0)) != cudaSuccess ||
-      (e = cudaStreamWaitEvent(h->stream, d2h[S & 1], 0)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(h->copy_out)) != cudaSuccess || (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+  for (int k = 0; k < kPipeSlots; ++k)
+    if ((e = cudaStreamWaitEvent(h->stream, d2h[k], 0)) != cudaSuccess) return cuda_error(e, "pipelined batch");
+  if ((e = cudaStreamSynchronize(h->copy_out)) != cudaSuccess || (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return cuda_error(e, "pipelined batch");
   int err = 0;
   for (int i = 0; i < S; ++i) {

@@ -72,6 +72,9 @@ int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io);
 // queued; completion is seen through Handle::done_event.  Used by the server.
 constexpr int kAsyncHostIO = 0x100;
 
+// Device slots of the pipelined host-memory path (sub-batches in flight).
+constexpr int kPipeSlots = 2;
+
 struct Handle {
   int device = 0;
   size_t budget = 0;
@@ -85,10 +88,10 @@ struct Handle {
   DeviceArena arena;
   DeviceArena arena3d;
   DeviceArena arena_bridge;
-  DeviceArena arena_pipe;                 // second slot of the pipelined host-memory path
+  DeviceArena arena_pipe[kPipeSlots - 1];  // further slots of the pipelined host-memory path
   cudaStream_t copy_in = nullptr;         // pipelined host-memory path: H2D stream
   cudaStream_t copy_out = nullptr;        // and D2H stream
-  cudaEvent_t pipe_events[6] = {};        // per slot: H2D done, kernels done, D2H done
+  cudaEvent_t pipe_events[3 * kPipeSlots] = {};  // per slot: H2D done, kernels done, D2H done
   PinnedBuf stage;
   PinnedBuf flags_host;
   PinnedBuf nt_host;
