@@ -38,8 +38,8 @@ BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
 STAGES_PER_STEP = 8
-# DRAM bytes per point of k_layers (both passes of one batch), from the ncu capture
-# summarised in profiles/k_layers_uneven256.md (read + write over 13.6M points);
+# DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
+# of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
 K_LAYERS_DRAM_BYTES_PER_POINT = 24.22
 
