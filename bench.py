@@ -15,6 +15,11 @@ far larger than the 129 MB L2, so no flush is needed between steps).
 * ``plain_*``: the same kernels one event per launch sequence.
 * ``cpu_baseline``: the oracle port (a C restatement of the reference serial
   algorithm, bit-identical to it) over all host cores on a bounded sample.
+* ``serving``: Poisson arrivals into the continuous-batching server and into
+  a one-event server, at a fixed load and at a load above the latter's
+  capacity; ``clue3d``: batched CLUE3D on 1,000 events of layer clusters;
+  ``hgcal_1000``: batched and plain on 1,000 HGCAL-occupancy events (about
+  325k points each).
 
 ``--impl reference`` times that CPU implementation alone on the same
 workload and prints the reference arm's line.
@@ -242,6 +247,44 @@ def serving_leg(C, b, rate, n_req, batched=True):
             "budget_bytes": 16 << 30, "max_inflight": 2 if batched else 1}
 
 
+def config2_leg(C, torch, stream, algo, args):
+    """HGCAL-occupancy events (100 layers x 50 blobs of 30-80 points + 500
+    noise points per layer, about 325k points each, seeds 1000 + e): the
+    batched form (device resident, graph replay) and the plain form (one
+    event per launch sequence) of the same kernels on the same events."""
+    from clue_gb300 import synthetic as S
+    b = S.hgcal_batch(args.config2_events, seed=1000)
+    off = b["offsets"]
+    E, N = off.size - 1, int(off[-1])
+    dev = {k: torch.from_numpy(b[k]).cuda() for k in ("x", "y", "layer", "weight")}
+    out = {k: torch.empty(N, dtype=torch.float32 if k in ("rho", "delta") else torch.int32, device="cuda")
+           for k in ("rho", "delta", "nearestHigher", "isSeed", "clusterIndex")}
+
+    def run(flags):
+        algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
+
+    def timed(flags, warm, steps):
+        for _ in range(warm):
+            run(flags)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            run(flags)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        algo.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_b = timed(0, 3, 3)
+    ms_p = timed(C.PLAIN, 1, 1)
+    del dev, out
+    torch.cuda.empty_cache()
+    return {"events": E, "points": N, "batched_events_per_s": E / (ms_b / 1000.0),
+            "batched_gpoints_per_s": N / (ms_b / 1000.0) / 1e9, "plain_events_per_s": E / (ms_p / 1000.0),
+            "batched_over_plain": ms_p / ms_b, "batched_ms_per_step": ms_b, "plain_ms_per_step": ms_p}
+
+
 def clue3d_leg(C, torch, stream, args):
     """Batched CLUE3D on synthetic layer clusters: 1000 events of 2k-20k
     clusters, 100 layers, +-2 sibling layers, criticalDensity 0.5."""
@@ -410,6 +453,9 @@ def run_gb300(args):
     clue3d = None
     if rank == 0 and not args.no_clue3d:
         clue3d = clue3d_leg(C, torch, stream, args)
+    config2 = None
+    if rank == 0 and not args.no_config2:
+        config2 = config2_leg(C, torch, stream, algo, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -427,7 +473,7 @@ def run_gb300(args):
                 "config": _config(args, b), "gpoints_per_s": gpts,
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
                 "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "serving": serving, "clue3d": clue3d,
+                "serving": serving, "clue3d": clue3d, "hgcal_1000": config2,
                 "clocks": clk.summary(), "gpu_launches": STAGES_PER_STEP * args.steps,
                 "tuning": algo.get_tuning()}
         print(json.dumps(line), flush=True)
@@ -457,6 +503,9 @@ def main():
                     help="second offered load (events/s) above the plain server's capacity; 0 = skip")
     ap.add_argument("--serving-requests", type=int, default=3000)
     ap.add_argument("--no-clue3d", action="store_true")
+    ap.add_argument("--no-config2", action="store_true",
+                    help="skip the batched-vs-plain measurement on HGCAL-occupancy events")
+    ap.add_argument("--config2-events", type=int, default=1000)
     ap.add_argument("--clue3d-events", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":
