@@ -247,7 +247,7 @@ def serving_leg(C, b, rate, n_req, batched=True):
             "budget_bytes": 16 << 30, "max_inflight": 2 if batched else 1}
 
 
-def config2_leg(C, torch, stream, algo, args):
+def config2_leg(C, torch, stream, args):
     """HGCAL-occupancy events (100 layers x 50 blobs of 30-80 points + 500
     noise points per layer, about 325k points each, seeds 1000 + e): the
     batched form (device resident, graph replay) and the plain form (one
@@ -259,6 +259,12 @@ def config2_leg(C, torch, stream, algo, args):
     dev = {k: torch.from_numpy(b[k]).cuda() for k in ("x", "y", "layer", "weight")}
     out = {k: torch.empty(N, dtype=torch.float32 if k in ("rho", "delta") else torch.int32, device="cuda")
            for k in ("rho", "delta", "nearestHigher", "isSeed", "clusterIndex")}
+    algo = C.Clusterizer(*PARAMS, budget_bytes=96 << 30, stream=stream.cuda_stream)
+    if not args.no_autotune:
+        # denser layers than the main workload: the decomposition is tuned for them
+        import tempfile
+        algo.autotune(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out,
+                      cache_path=os.path.join(tempfile.gettempdir(), "clue_gb300_autotune.jsonl"))
 
     def run(flags):
         algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
@@ -278,11 +284,14 @@ def config2_leg(C, torch, stream, algo, args):
 
     ms_b = timed(0, 3, 3)
     ms_p = timed(C.PLAIN, 1, 1)
+    tuning = algo.get_tuning()
+    algo.close()
     del dev, out
     torch.cuda.empty_cache()
     return {"events": E, "points": N, "batched_events_per_s": E / (ms_b / 1000.0),
             "batched_gpoints_per_s": N / (ms_b / 1000.0) / 1e9, "plain_events_per_s": E / (ms_p / 1000.0),
-            "batched_over_plain": ms_p / ms_b, "batched_ms_per_step": ms_b, "plain_ms_per_step": ms_p}
+            "batched_over_plain": ms_p / ms_b, "batched_ms_per_step": ms_b, "plain_ms_per_step": ms_p,
+            "tuning": tuning}
 
 
 def clue3d_leg(C, torch, stream, args):
@@ -455,7 +464,7 @@ def run_gb300(args):
         clue3d = clue3d_leg(C, torch, stream, args)
     config2 = None
     if rank == 0 and not args.no_config2:
-        config2 = config2_leg(C, torch, stream, algo, args)
+        config2 = config2_leg(C, torch, stream, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -99,7 +99,7 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
     // Stage 1: the first pass (threads, on-chip capacity) with the handle's
     // second pass; stage 2 (below): the second pass for the stage-1 winner.
     std::vector<Tuning2D> cands;
-    const int caps[] = {1024, 1536, 2048, 2560};
+    const int caps[] = {1024, 1536, 2048, 2560, 3072, 4096};
     const int threads[] = {128, 256, 512};
     for (int th : threads)
       for (int cap : caps) {
