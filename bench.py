@@ -42,7 +42,7 @@ METRIC = "CLUE events/s & Gpoints/s, batched vs plain on 1 GB300 (bit-exact); p9
 BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
-STAGES_PER_STEP = 8
+STAGES_PER_STEP = 8   # kernels of one batch, plus the large-layer pass when the tuning has one
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
@@ -373,6 +373,10 @@ def run_gb300(args):
     def run(flags):
         algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
 
+    t_now = algo.get_tuning()
+    launches_per_step = STAGES_PER_STEP + (1 if t_now["big_threads"] > 0 and
+                                           t_now["big_capacity"] > t_now["layer_capacity"] else 0)
+
     # ---- batched, device resident (headline value)
     for _ in range(args.warmup):
         run(0)
@@ -483,7 +487,7 @@ def run_gb300(args):
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
                 "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "serving": serving, "clue3d": clue3d, "hgcal_1000": config2,
-                "clocks": clk.summary(), "gpu_launches": STAGES_PER_STEP * args.steps,
+                "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "tuning": algo.get_tuning()}
         print(json.dumps(line), flush=True)
     algo.close()
