@@ -173,11 +173,50 @@ __global__ void k3_row_sort(Batch3D b) {
   }
   b.sorted[s + rank] = idx;
   b.scol[s + rank] = col;
+  // occupancy of the row's phi columns; bit 127 marks a column held twice
+  unsigned long long* m = b.row_mask + 2 * r;
+  const unsigned long long bit = 1ull << (col & 63);
+  if (atomicOr(m + (col >> 6), bit) & bit) atomicOr(m + 1, 1ull << 63);
 }
 
 // Visits the entries of one row whose phi column lies in the window
 // [p0, p1] (p0 may be negative, p1 may exceed 125), in the reference's
 // order: iphi_it = p0..p1 mapped modulo 126.
+// Entries of a row whose phi column lies in [a, c] (0 <= a <= c <= 125) are
+// one run of the row (entries are sorted by column): its first position and
+// length, from the column-occupancy mask, when no column repeats.
+__device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long long m1, int p) {
+  // set bits of columns < p (0 <= p <= 126)
+  if (p <= 0) return 0;
+  if (p < 64) return __popcll(m0 & ((1ull << p) - 1));
+  return __popcll(m0) + __popcll(m1 & ((1ull << (p - 64)) - 1));
+}
+
+// visit_row() for row r through its occupancy mask: the row start is read
+// only when the window holds an entry, and the row is not scanned.
+template <class F>
+__device__ __forceinline__ void visit_row_masked(const Batch3D& b, int64_t r, int p0, int p1, F&& f) {
+  const unsigned long long m0 = b.row_mask[2 * r], m1 = b.row_mask[2 * r + 1];
+  if (m1 >> 63) {  // a column holds several entries: walk the row
+    visit_row(b, b.row_start[r], b.row_start[r + 1], p0, p1, f);
+    return;
+  }
+  int a0, c0, a1 = 0, c1 = -1;  // first run [a0, c0], then [a1, c1] (wrapping windows)
+  if (p0 >= 0 && p1 < kPhiBins) {
+    a0 = p0; c0 = p1;
+  } else if (p0 < 0) {
+    a0 = p0 + kPhiBins; c0 = kPhiBins - 1; a1 = 0; c1 = p1;
+  } else {
+    a0 = p0; c0 = kPhiBins - 1; a1 = 0; c1 = p1 - kPhiBins;
+  }
+  const int lo0 = bits_below(m0, m1, a0), n0 = bits_below(m0, m1, c0 + 1) - lo0;
+  const int n1 = c1 >= a1 ? bits_below(m0, m1, c1 + 1) : 0;  // the second run starts at column 0
+  if (n0 + n1 == 0) return;
+  const int s = b.row_start[r];
+  for (int q = s + lo0; q < s + lo0 + n0; ++q) f(b.sorted[q]);
+  for (int q = s; q < s + n1; ++q) f(b.sorted[q]);
+}
+
 template <class F>
 __device__ __forceinline__ void visit_row(const Batch3D& b, int s, int t, int p0, int p1, F&& f) {
   if (p0 >= 0 && p1 < kPhiBins) {
@@ -228,7 +267,7 @@ __global__ void k3_density(Batch3D b, Params3D P) {
     const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
       const int64_t r = rbase + (int64_t)cl * kEtaBins + ie;
-      visit_row(b, b.row_start[r], b.row_start[r + 1], pb - 2, pb + 2, [&](int j) {
+      visit_row_masked(b, r, pb - 2, pb + 2, [&](int j) {
         const int64_t gj = es + j;
         const float r1 = __fmul_rn(b.roa[gj], zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, b.phi[gj]), P);
@@ -264,7 +303,7 @@ __global__ void k3_nh(Batch3D b, Params3D P) {
     const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
       const int64_t r = rbase + (int64_t)cl * kEtaBins + ie;
-      visit_row(b, b.row_start[r], b.row_start[r + 1], pb - 1, pb + 1, [&](int j) {
+      visit_row_masked(b, r, pb - 1, pb + 1, [&](int j) {
         const int64_t gj = es + j;
         const float r1 = __fmul_rn(b.roa[gj], zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, b.phi[gj]), P);
@@ -375,6 +414,8 @@ __global__ void __launch_bounds__(512) k3_finish(Batch3D b) {
 cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   if (b.n_events <= 0 || b.n_points <= 0) return cudaSuccess;
   cudaError_t err = cudaMemsetAsync(b.row_cnt, 0, sizeof(int32_t) * (size_t)b.n_events * b.n_rows, s);
+  if (err != cudaSuccess) return err;
+  err = cudaMemsetAsync(b.row_mask, 0, 16 * (size_t)b.n_events * b.n_rows, s);
   if (err != cudaSuccess) return err;
   const int T = 256;
   const int grid = (int)((b.n_points + T - 1) / T);
