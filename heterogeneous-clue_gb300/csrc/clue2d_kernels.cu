@@ -671,20 +671,25 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   sm.nh = reinterpret_cast<int32_t*>(sm.rec + cap);
   sm.qord = reinterpret_cast<uint16_t*>(sm.nh + cap);
   int32_t* big_list = b.cursor;  // k_scatter's cursors are dead by now
-  for (;;) {
-    if (threadIdx.x == 0) {
-      if (!big_pass) {
-        const int t = atomicAdd(&b.flags[kFlagTicket], 1);
-        s_item = t < n_items ? t : -1;
-      } else {
-        const int t = atomicAdd(&b.flags[kFlagTicket2], 1);
-        s_item = t < b.flags[kFlagBigCount] ? big_list[t] : -1;
-      }
+  // The next ticket is taken as soon as the current item is known and only
+  // published at the next iteration, so the atomic's round trip overlaps the
+  // current layer instead of holding the whole CTA at a barrier.
+  auto fetch = [&]() {
+    if (!big_pass) {
+      const int t = atomicAdd(&b.flags[kFlagTicket], 1);
+      return t < n_items ? t : -1;
     }
+    const int t = atomicAdd(&b.flags[kFlagTicket2], 1);
+    return t < b.flags[kFlagBigCount] ? big_list[t] : -1;
+  };
+  int next = threadIdx.x == 0 ? fetch() : -1;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = next;
     __syncthreads();
     const int item = s_item;
     __syncthreads();
     if (item < 0) break;
+    if (threadIdx.x == 0) next = fetch();
     const int m = b.lcnt[item];
     if (m == 0) continue;
     if (m > max_m) {  // first pass: leave it to the large-capacity pass
