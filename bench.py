@@ -46,7 +46,7 @@ STAGES_PER_STEP = 8   # kernels of one batch, plus the large-layer pass when the
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
-K_LAYERS_DRAM_BYTES_PER_POINT = 24.22
+K_LAYERS_DRAM_BYTES_PER_POINT = 24.24
 
 
 def _dist():
