@@ -47,6 +47,11 @@ STAGES_PER_STEP = 8   # kernels of one batch, plus the large-layer pass when the
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
 K_LAYERS_DRAM_BYTES_PER_POINT = 24.24
+# Warp instructions per point of k_layers (both passes), same capture: the
+# kernel is bound by instruction issue, so its issue rate against the SMs'
+# peak (4 schedulers x 1 instruction per cycle) is the bound that applies.
+K_LAYERS_WARP_INST_PER_POINT = 100.9
+
 
 
 def _dist():
@@ -407,6 +412,7 @@ def run_gb300(args):
     stage_ms = {k: v / prof_steps for k, v in stage_sum.items()}
     peak, peak_kind = _peak_hbm()
     layers_ms = stage_ms["layers"]
+    clocks = clk.summary()
     achieved = BYTES_PER_POINT * N / (layers_ms / 1000.0) / 1e9
     pipe_achieved = BYTES_PER_POINT * N / (ms_step / 1000.0) / 1e9
     traffic = K_LAYERS_DRAM_BYTES_PER_POINT * N
@@ -415,6 +421,13 @@ def run_gb300(args):
                 "algorithmic_bytes_per_point": BYTES_PER_POINT,
                 "pipeline_achieved": pipe_achieved, "pipeline_frac": pipe_achieved / peak,
                 "compulsory_frac": COMPULSORY_BYTES_PER_POINT * N / (ms_step / 1000.0) / 1e9 / peak}
+    props = torch.cuda.get_device_properties(local)
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    issue_peak = props.multi_processor_count * 4 * mhz * 1e6
+    issue_achieved = K_LAYERS_WARP_INST_PER_POINT * N / (layers_ms / 1000.0)
+    roofline["issue"] = {"warp_instructions_per_point": K_LAYERS_WARP_INST_PER_POINT,
+                         "achieved_warp_inst_per_s": issue_achieved, "peak_warp_inst_per_s": issue_peak,
+                         "frac": issue_achieved / issue_peak, "sm_mhz": mhz}
 
     # ---- plain: the same kernels, one event per launch sequence
     plain = None
@@ -487,7 +500,7 @@ def run_gb300(args):
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
                 "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "serving": serving, "clue3d": clue3d, "hgcal_1000": config2,
-                "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+                "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
                 "tuning": algo.get_tuning()}
         print(json.dumps(line), flush=True)
     algo.close()
