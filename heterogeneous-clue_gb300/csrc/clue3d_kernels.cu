@@ -281,7 +281,7 @@ __global__ void k3_density(Batch3D b, Params3D P) {
   b.rho[gi] = rho;
 }
 
-__global__ void k3_nh(Batch3D b, Params3D P) {
+__global__ void __launch_bounds__(256, 5) k3_nh(Batch3D b, Params3D P) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= b.n_points) return;
   const int e = event_of(b.offsets, b.n_events, p);
