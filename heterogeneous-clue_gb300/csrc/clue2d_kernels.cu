@@ -922,13 +922,21 @@ int layer_grid(const Tuning2D& t, int n_items) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int per_sm = t.ctas_per_sm;
   if (per_sm <= 0) {
-    int smem_sm = 0;
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    const size_t need = layer_smem_bytes(t) + 1024 + 256;  // + static smem and per-CTA reserve
-    per_sm = (int)(smem_sm / need);
+    // resident CTAs per SM as the hardware sees them (registers, shared memory, threads)
+    const size_t smem = layer_smem_bytes(t);
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (t.threads) {
+      case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_layers<128>, 128, smem); break;
+      case 256: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_layers<256>, 256, smem); break;
+      case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_layers<512>, 512, smem); break;
+      case 1024: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_layers<1024>, 1024, smem); break;
+      default: break;
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
     per_sm = per_sm < 1 ? 1 : per_sm;
-    const int by_threads = 2048 / t.threads;
-    per_sm = per_sm > by_threads ? by_threads : per_sm;
   }
   int g = sms * per_sm;
   if (g > n_items) g = n_items;

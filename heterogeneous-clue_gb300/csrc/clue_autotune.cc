@@ -190,6 +190,10 @@ extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, con
       h->tuning = saved;
       return rc;
     }
+    if (best.big_threads > 0 && best.big_capacity <= best.layer_capacity) {
+      best.big_threads = 0;  // the second pass takes no layer with this capacity: say so
+      best.big_capacity = 0;
+    }
     h->tuning = best;
     cache_store(cache_path, gpu, key, best, best_ms);
   }
