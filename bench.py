@@ -157,6 +157,23 @@ def time_cpu(b, n_sample, threads):
                 gpoints_per_s=smp["offsets"][-1] / dt / 1e9)
 
 
+def time_cpu_single(reps=3):
+    """Single-thread latency of the CPU implementation on one toy-detector
+    event (100k points) and one HGCAL-occupancy event (about 325k points):
+    the best of ``reps`` runs, input generation excluded."""
+    import oracle
+    from clue_gb300 import synthetic as S
+    res = {}
+    for name, ev in (("toy_100k", S.toy_event(12345)), ("hgcal_event", S.hgcal_event(1000))):
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *PARAMS)
+            best = min(best, time.perf_counter() - t0)
+        res[name] = {"points": int(ev["x"].size), "ms": 1000.0 * best}
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -490,7 +507,7 @@ def run_gb300(args):
         cpu = {"value": r["events_per_s"], "unit": "events/s", "cores": threads, "kind": "port",
                "sample": f"{r['events']} events strided over the workload ({r['points']} points), "
                          f"{r['seconds']:.1f} s on {threads} threads",
-               "gpoints_per_s": r["gpoints_per_s"]}
+               "gpoints_per_s": r["gpoints_per_s"], "single_thread_latency": time_cpu_single()}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": ws, "steps": args.steps,
