@@ -496,6 +496,37 @@ def run_gb300(args):
     clue3d = None
     if rank == 0 and not args.no_clue3d:
         clue3d = clue3d_leg(C, torch, stream, args)
+    # ---- one event alone: the reference producer's call (toy-detector event, 100k points)
+    single = None
+    if rank == 0:
+        from clue_gb300 import synthetic as S
+        ev = S.toy_event(12345)
+        n1 = ev["x"].size
+        one = C.Clusterizer(*PARAMS, budget_bytes=4 << 30, stream=stream.cuda_stream)
+        for _ in range(3):
+            one.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
+        t0 = time.perf_counter()
+        for _ in range(20):
+            one.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
+        host_ms = (time.perf_counter() - t0) / 20 * 1000.0
+        d1 = {k: torch.from_numpy(ev[k]).cuda() for k in ("x", "y", "layer", "weight")}
+        o1 = {k: torch.empty(n1, dtype=torch.float32 if k in ("rho", "delta") else torch.int32, device="cuda")
+              for k in ("rho", "delta", "nearestHigher", "isSeed", "clusterIndex")}
+        off1 = np.array([0, n1], np.int64)
+        for _ in range(3):
+            one.run_batch(off1, d1["x"], d1["y"], d1["layer"], d1["weight"], out=o1, flags=C.DEVICE_MEMORY)
+        one.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(20):
+            one.run_batch(off1, d1["x"], d1["y"], d1["layer"], d1["weight"], out=o1, flags=C.DEVICE_MEMORY)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        one.synchronize()
+        one.close()
+        single = {"event": "toy-detector, 100,000 points", "host_memory_ms": host_ms,
+                  "device_memory_ms": s0.elapsed_time(s1) / 20}
+
     config2 = None
     if rank == 0 and not args.no_config2:
         config2 = config2_leg(C, torch, stream, args)
@@ -516,7 +547,7 @@ def run_gb300(args):
                 "config": _config(args, b), "gpoints_per_s": gpts,
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
                 "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "serving": serving, "clue3d": clue3d, "hgcal_1000": config2,
+                "serving": serving, "clue3d": clue3d, "hgcal_1000": config2, "single_event": single,
                 "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
                 "tuning": algo.get_tuning()}
         print(json.dumps(line), flush=True)
