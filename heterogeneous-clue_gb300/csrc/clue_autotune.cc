@@ -84,126 +84,128 @@ using namespace clue;
 extern "C" int clue_autotune(clue_handle* hh, int32_t E, const int64_t* off, const float* x, const float* y,
                              const int32_t* layer, const float* w, const clue_outputs* out, const char* cache_path,
                              clue_tuning* chosen) {
-  if (!hh || !off || !out) return set_error(CLUE_EINVAL, "NULL argument");
-  if (E <= 0) return set_error(CLUE_EINVAL, "n_events must be > 0");
-  Handle* h = reinterpret_cast<Handle*>(hh);
-  cudaSetDevice(h->device);
-  const std::string gpu = gpu_name(h->device);
-  const std::string key = workload_key(E, off, h->p2d);
-  Tuning2D best = h->tuning;
-  if (cache_lookup(cache_path, gpu, key, &best)) {
-    h->tuning = best;
-  } else {
-    int smem_optin = 0;
-    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    // Stage 1: the first pass (threads, on-chip capacity) with the handle's
-    // second pass; stage 2 (below): the second pass for the stage-1 winner.
-    std::vector<Tuning2D> cands;
-    const int caps[] = {1024, 1536, 2048, 2560, 3072, 4096};
-    const int threads[] = {128, 256, 512};
-    for (int th : threads)
-      for (int cap : caps) {
-        Tuning2D t;
-        t.threads = th;
-        t.layer_capacity = cap;
-        t.work_tile_cm = 0.f;
-        t.ctas_per_sm = 0;
-        t.big_threads = h->tuning.big_threads;
-        t.big_capacity = h->tuning.big_capacity;
-        if (layer_smem_bytes(t) + 1024 > (size_t)smem_optin) continue;
-        cands.push_back(t);
-      }
-    const size_t stage1 = cands.size();
-    const int big[][2] = {{512, 8192}, {512, 4096}, {256, 4096}, {512, 2560}, {256, 2560}, {0, 0}};
-    unsigned long long* d_dig = nullptr;
-    if (cudaMalloc(&d_dig, sizeof(unsigned long long)) != cudaSuccess) {
-      cudaGetLastError();
-      return set_error(CLUE_ENOMEM, "autotune digest buffer");
-    }
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
-    const int64_t N = off[E];
-    unsigned long long ref_digest = 0;
-    float best_ms = 1e30f;
-    int rc = CLUE_OK;
-    const Tuning2D saved = h->tuning;
-    for (size_t ci = 0; rc == CLUE_OK; ++ci) {
-      if (ci == stage1) {  // stage 2: second-pass variants of the stage-1 winner
-        for (const auto& bp : big) {
-          Tuning2D t = best;
-          t.big_threads = bp[0];
-          t.big_capacity = bp[1];
-          if (bp[0] && t.big_capacity <= t.layer_capacity) continue;
-          if (t.big_threads == best.big_threads && t.big_capacity == best.big_capacity) continue;
-          if (bp[0] && layer_smem_bytes(Tuning2D{t.big_threads, t.big_capacity}) + 1024 > (size_t)smem_optin) continue;
+  return clue::guarded([&]() -> int {
+    if (!hh || !off || !out) return set_error(CLUE_EINVAL, "NULL argument");
+    if (E <= 0) return set_error(CLUE_EINVAL, "n_events must be > 0");
+    Handle* h = reinterpret_cast<Handle*>(hh);
+    cudaSetDevice(h->device);
+    const std::string gpu = gpu_name(h->device);
+    const std::string key = workload_key(E, off, h->p2d);
+    Tuning2D best = h->tuning;
+    if (cache_lookup(cache_path, gpu, key, &best)) {
+      h->tuning = best;
+    } else {
+      int smem_optin = 0;
+      cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+      // Stage 1: the first pass (threads, on-chip capacity) with the handle's
+      // second pass; stage 2 (below): the second pass for the stage-1 winner.
+      std::vector<Tuning2D> cands;
+      const int caps[] = {1024, 1536, 2048, 2560, 3072, 4096};
+      const int threads[] = {128, 256, 512};
+      for (int th : threads)
+        for (int cap : caps) {
+          Tuning2D t;
+          t.threads = th;
+          t.layer_capacity = cap;
+          t.work_tile_cm = 0.f;
+          t.ctas_per_sm = 0;
+          t.big_threads = h->tuning.big_threads;
+          t.big_capacity = h->tuning.big_capacity;
+          if (layer_smem_bytes(t) + 1024 > (size_t)smem_optin) continue;
           cands.push_back(t);
         }
+      const size_t stage1 = cands.size();
+      const int big[][2] = {{512, 8192}, {512, 4096}, {256, 4096}, {512, 2560}, {256, 2560}, {0, 0}};
+      unsigned long long* d_dig = nullptr;
+      if (cudaMalloc(&d_dig, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(CLUE_ENOMEM, "autotune digest buffer");
       }
-      if (ci >= cands.size()) break;
-      h->tuning = cands[ci];
-      const int flags = CLUE_DEVICE_MEMORY | CLUE_NO_GRAPH;
-      rc = h->run_batch(E, off, x, y, layer, w, out, flags);  // warm-up (and allocation)
-      if (rc) break;
-      const int reps = 3;
-      cudaEventRecord(t0, h->stream);
-      for (int r = 0; r < reps && rc == CLUE_OK; ++r) rc = h->run_batch(E, off, x, y, layer, w, out, flags);
-      cudaEventRecord(t1, h->stream);
-      if (rc) break;
-      cudaEventSynchronize(t1);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, t0, t1);
-      ms /= reps;
-      // digest all five outputs
-      cudaMemsetAsync(d_dig, 0, sizeof(unsigned long long), h->stream);
-      launch_digest(out->rho, N, d_dig, h->stream);
-      launch_digest(out->delta, N, d_dig, h->stream);
-      launch_digest(out->nearestHigher, N, d_dig, h->stream);
-      launch_digest(out->isSeed, N, d_dig, h->stream);
-      launch_digest(out->clusterIndex, N, d_dig, h->stream);
-      unsigned long long dig = 0;
-      cudaMemcpyAsync(&dig, d_dig, sizeof(dig), cudaMemcpyDeviceToHost, h->stream);
-      cudaError_t e = cudaStreamSynchronize(h->stream);
-      if (e != cudaSuccess) {
-        rc = cuda_error(e, "autotune");
-        break;
+      cudaEvent_t t0, t1;
+      cudaEventCreate(&t0);
+      cudaEventCreate(&t1);
+      const int64_t N = off[E];
+      unsigned long long ref_digest = 0;
+      float best_ms = 1e30f;
+      int rc = CLUE_OK;
+      const Tuning2D saved = h->tuning;
+      for (size_t ci = 0; rc == CLUE_OK; ++ci) {
+        if (ci == stage1) {  // stage 2: second-pass variants of the stage-1 winner
+          for (const auto& bp : big) {
+            Tuning2D t = best;
+            t.big_threads = bp[0];
+            t.big_capacity = bp[1];
+            if (bp[0] && t.big_capacity <= t.layer_capacity) continue;
+            if (t.big_threads == best.big_threads && t.big_capacity == best.big_capacity) continue;
+            if (bp[0] && layer_smem_bytes(Tuning2D{t.big_threads, t.big_capacity}) + 1024 > (size_t)smem_optin) continue;
+            cands.push_back(t);
+          }
+        }
+        if (ci >= cands.size()) break;
+        h->tuning = cands[ci];
+        const int flags = CLUE_DEVICE_MEMORY | CLUE_NO_GRAPH;
+        rc = h->run_batch(E, off, x, y, layer, w, out, flags);  // warm-up (and allocation)
+        if (rc) break;
+        const int reps = 3;
+        cudaEventRecord(t0, h->stream);
+        for (int r = 0; r < reps && rc == CLUE_OK; ++r) rc = h->run_batch(E, off, x, y, layer, w, out, flags);
+        cudaEventRecord(t1, h->stream);
+        if (rc) break;
+        cudaEventSynchronize(t1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        ms /= reps;
+        // digest all five outputs
+        cudaMemsetAsync(d_dig, 0, sizeof(unsigned long long), h->stream);
+        launch_digest(out->rho, N, d_dig, h->stream);
+        launch_digest(out->delta, N, d_dig, h->stream);
+        launch_digest(out->nearestHigher, N, d_dig, h->stream);
+        launch_digest(out->isSeed, N, d_dig, h->stream);
+        launch_digest(out->clusterIndex, N, d_dig, h->stream);
+        unsigned long long dig = 0;
+        cudaMemcpyAsync(&dig, d_dig, sizeof(dig), cudaMemcpyDeviceToHost, h->stream);
+        cudaError_t e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+          rc = cuda_error(e, "autotune");
+          break;
+        }
+        rc = h->check_device_flags();
+        if (rc) break;
+        if (ci == 0) {
+          ref_digest = dig;
+        } else if (dig != ref_digest) {
+          rc = set_error(CLUE_ECUDA,
+                         "autotune: candidate (threads %d, capacity %d, second pass %d x %d) changed the outputs",
+                         cands[ci].threads, cands[ci].layer_capacity, cands[ci].big_threads, cands[ci].big_capacity);
+          break;
+        }
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = cands[ci];
+        }
       }
-      rc = h->check_device_flags();
-      if (rc) break;
-      if (ci == 0) {
-        ref_digest = dig;
-      } else if (dig != ref_digest) {
-        rc = set_error(CLUE_ECUDA,
-                       "autotune: candidate (threads %d, capacity %d, second pass %d x %d) changed the outputs",
-                       cands[ci].threads, cands[ci].layer_capacity, cands[ci].big_threads, cands[ci].big_capacity);
-        break;
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      cudaFree(d_dig);
+      if (rc) {
+        h->tuning = saved;
+        return rc;
       }
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = cands[ci];
+      if (best.big_threads > 0 && best.big_capacity <= best.layer_capacity) {
+        best.big_threads = 0;  // the second pass takes no layer with this capacity: say so
+        best.big_capacity = 0;
       }
+      h->tuning = best;
+      cache_store(cache_path, gpu, key, best, best_ms);
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    cudaFree(d_dig);
-    if (rc) {
-      h->tuning = saved;
-      return rc;
+    if (chosen) {
+      chosen->threads = best.threads;
+      chosen->layer_capacity = best.layer_capacity;
+      chosen->work_tile_cm = best.work_tile_cm;
+      chosen->ctas_per_sm = best.ctas_per_sm;
+      chosen->big_threads = best.big_threads;
+      chosen->big_capacity = best.big_capacity;
     }
-    if (best.big_threads > 0 && best.big_capacity <= best.layer_capacity) {
-      best.big_threads = 0;  // the second pass takes no layer with this capacity: say so
-      best.big_capacity = 0;
-    }
-    h->tuning = best;
-    cache_store(cache_path, gpu, key, best, best_ms);
-  }
-  if (chosen) {
-    chosen->threads = best.threads;
-    chosen->layer_capacity = best.layer_capacity;
-    chosen->work_tile_cm = best.work_tile_cm;
-    chosen->ctas_per_sm = best.ctas_per_sm;
-    chosen->big_threads = best.big_threads;
-    chosen->big_capacity = best.big_capacity;
-  }
-  return CLUE_OK;
+    return CLUE_OK;
+  });
 }

@@ -140,109 +140,113 @@ extern "C" {
 
 int clue_bridge_count(clue_handle* hh, int32_t E, const int64_t* off, const int32_t* isSeed,
                       int64_t* cluster_offsets) {
-  if (!hh || !cluster_offsets) return set_error(CLUE_EINVAL, "NULL argument");
-  int rc = clue::check_offsets(E, off, "event_offsets");
-  if (rc) return rc;
-  cluster_offsets[0] = 0;
-  if (E == 0) return CLUE_OK;
-  const int64_t N = off[E];
-  if (N > 0 && !isSeed) return set_error(CLUE_EINVAL, "isSeed is NULL");
-  Handle* h = reinterpret_cast<Handle*>(hh);
-  cudaError_t e = cudaSetDevice(h->device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  if ((rc = h->wait_previous())) return rc;
-  std::vector<size_t> need(clue::B_SLOTS, 0);
-  need[clue::B_OFF] = 8 * (size_t)(E + 1);
-  need[clue::B_COUNT] = 4 * (size_t)E;
-  if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
-  if ((rc = h->stage.reserve(8 * (size_t)(E + 1)))) return rc;
-  auto P = [&](int s) { return h->arena_bridge.ptr(s); };
-  cudaStream_t s = h->stream;
-  memcpy(h->stage.p, off, 8 * (size_t)(E + 1));
-  if ((e = cudaMemcpyAsync(P(clue::B_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
-      (e = cudaMemsetAsync(P(clue::B_COUNT), 0, 4 * (size_t)E, s)))
-    return cuda_error(e, "bridge set-up");
-  if (N > 0)
-    clue::k_bridge_count<<<clue::grid_for(N), 256, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
-                                                            isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
-  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_count");
-  std::vector<int32_t> counts(E);
-  if ((e = cudaMemcpyAsync(counts.data(), P(clue::B_COUNT), 4 * (size_t)E, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaStreamSynchronize(s)))
-    return cuda_error(e, "bridge counts");
-  for (int32_t i = 0; i < E; ++i) cluster_offsets[i + 1] = cluster_offsets[i] + counts[i];
-  return CLUE_OK;
+  return clue::guarded([&]() -> int {
+    if (!hh || !cluster_offsets) return set_error(CLUE_EINVAL, "NULL argument");
+    int rc = clue::check_offsets(E, off, "event_offsets");
+    if (rc) return rc;
+    cluster_offsets[0] = 0;
+    if (E == 0) return CLUE_OK;
+    const int64_t N = off[E];
+    if (N > 0 && !isSeed) return set_error(CLUE_EINVAL, "isSeed is NULL");
+    Handle* h = reinterpret_cast<Handle*>(hh);
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    if ((rc = h->wait_previous())) return rc;
+    std::vector<size_t> need(clue::B_SLOTS, 0);
+    need[clue::B_OFF] = 8 * (size_t)(E + 1);
+    need[clue::B_COUNT] = 4 * (size_t)E;
+    if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
+    if ((rc = h->stage.reserve(8 * (size_t)(E + 1)))) return rc;
+    auto P = [&](int s) { return h->arena_bridge.ptr(s); };
+    cudaStream_t s = h->stream;
+    memcpy(h->stage.p, off, 8 * (size_t)(E + 1));
+    if ((e = cudaMemcpyAsync(P(clue::B_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(P(clue::B_COUNT), 0, 4 * (size_t)E, s)))
+      return cuda_error(e, "bridge set-up");
+    if (N > 0)
+      clue::k_bridge_count<<<clue::grid_for(N), 256, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
+                                                              isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
+    if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_count");
+    std::vector<int32_t> counts(E);
+    if ((e = cudaMemcpyAsync(counts.data(), P(clue::B_COUNT), 4 * (size_t)E, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return cuda_error(e, "bridge counts");
+    for (int32_t i = 0; i < E; ++i) cluster_offsets[i + 1] = cluster_offsets[i] + counts[i];
+    return CLUE_OK;
+  });
 }
 
 int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, const int64_t* off, const float* x,
                       const float* y, const int32_t* layer, const float* weight, const int32_t* isSeed,
                       const int32_t* clusterIndex, const int64_t* coff, const clue_layer_clusters* out) {
-  if (!hh || !p || !out) return set_error(CLUE_EINVAL, "NULL argument");
-  int rc = clue::check_offsets(E, off, "event_offsets");
-  if (rc) return rc;
-  if ((rc = clue::check_offsets(E, coff, "cluster_offsets"))) return rc;
-  if (p->n_layers < 1 || !p->layer_z) return set_error(CLUE_EINVAL, "bridge needs n_layers >= 1 and a z table");
-  if (E == 0) return CLUE_OK;
-  const int64_t N = off[E], C = coff[E];
-  if (N > 0 && (!x || !y || !layer || !weight || !isSeed || !clusterIndex))
-    return set_error(CLUE_EINVAL, "NULL input array");
-  const void* outs[10] = {out->x, out->y, out->z, out->eta, out->phi, out->r_over_absz, out->radius,
-                          out->layer, out->energy, out->isSilicon};
-  if (C > 0)
-    for (auto q : outs)
-      if (!q) return set_error(CLUE_EINVAL, "NULL output array");
-  Handle* h = reinterpret_cast<Handle*>(hh);
-  cudaError_t e = cudaSetDevice(h->device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  if ((rc = h->wait_previous())) return rc;
-  std::vector<size_t> need(clue::B_SLOTS, 0);
-  need[clue::B_OFF] = need[clue::B_COFF] = 8 * (size_t)(E + 1);
-  need[clue::B_COUNT] = 4 * (size_t)E;
-  need[clue::B_ACC] = 24 * (size_t)std::max<int64_t>(C, 1);
-  need[clue::B_SEED] = 4 * (size_t)std::max<int64_t>(C, 1);
-  need[clue::B_LZ] = 4 * (size_t)p->n_layers;
-  need[clue::B_FLAGS] = 4 * clue::kFlagCount;
-  if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
-  const size_t stage_bytes = 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers;
-  if ((rc = h->stage.reserve(stage_bytes))) return rc;
-  if ((rc = h->flags_host.reserve(4 * clue::kFlagCount))) return rc;
-  auto P = [&](int s) { return h->arena_bridge.ptr(s); };
-  char* st = static_cast<char*>(h->stage.p);
-  memcpy(st, off, 8 * (size_t)(E + 1));
-  memcpy(st + 8 * (size_t)(E + 1), coff, 8 * (size_t)(E + 1));
-  memcpy(st + 16 * (size_t)(E + 1), p->layer_z, 4 * (size_t)p->n_layers);
-  cudaStream_t s = h->stream;
-  if ((e = cudaMemcpyAsync(P(clue::B_OFF), st, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
-      (e = cudaMemcpyAsync(P(clue::B_COFF), st + 8 * (size_t)(E + 1), 8 * (size_t)(E + 1), cudaMemcpyHostToDevice,
-                           s)) ||
-      (e = cudaMemcpyAsync(P(clue::B_LZ), st + 16 * (size_t)(E + 1), 4 * (size_t)p->n_layers,
-                           cudaMemcpyHostToDevice, s)) ||
-      (e = cudaMemsetAsync(P(clue::B_ACC), 0, 24 * (size_t)std::max<int64_t>(C, 1), s)) ||
-      (e = cudaMemsetAsync(P(clue::B_SEED), 0, 4 * (size_t)std::max<int64_t>(C, 1), s)) ||
-      (e = cudaMemsetAsync(P(clue::B_FLAGS), 0, 4 * clue::kFlagCount, s)))
-    return cuda_error(e, "bridge set-up");
-  int32_t* flags = static_cast<int32_t*>(P(clue::B_FLAGS));
-  auto* acc = static_cast<unsigned long long*>(P(clue::B_ACC));
-  auto* seed_of = static_cast<int32_t*>(P(clue::B_SEED));
-  if (N > 0)
-    clue::k_bridge_accumulate<<<clue::grid_for(N), 256, 0, s>>>(
-        E, N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int64_t*>(P(clue::B_COFF)), x, y,
-        weight, isSeed, clusterIndex, acc, seed_of, flags);
-  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_accumulate");
-  if (C > 0)
-    clue::k_bridge_finalize<<<clue::grid_for(C), 256, 0, s>>>(C, acc, seed_of, x, y, layer,
-                                                               static_cast<const float*>(P(clue::B_LZ)),
-                                                               p->n_layers, p->radius, p->isSilicon, *out, flags);
-  if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_finalize");
-  if ((e = cudaMemcpyAsync(h->flags_host.p, flags, 4 * clue::kFlagCount, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaStreamSynchronize(s)))
-    return cuda_error(e, "bridge");
-  int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
-  const int32_t err = fh[clue::kFlagError];
-  fh[clue::kFlagError] = 0;
-  if (err == 1) return set_error(CLUE_EINVAL, "a clusterIndex is not below its event's cluster count");
-  if (err == 2) return set_error(CLUE_EINVAL, "a layer cluster's layer is outside [0, %d)", p->n_layers);
-  return CLUE_OK;
+  return clue::guarded([&]() -> int {
+    if (!hh || !p || !out) return set_error(CLUE_EINVAL, "NULL argument");
+    int rc = clue::check_offsets(E, off, "event_offsets");
+    if (rc) return rc;
+    if ((rc = clue::check_offsets(E, coff, "cluster_offsets"))) return rc;
+    if (p->n_layers < 1 || !p->layer_z) return set_error(CLUE_EINVAL, "bridge needs n_layers >= 1 and a z table");
+    if (E == 0) return CLUE_OK;
+    const int64_t N = off[E], C = coff[E];
+    if (N > 0 && (!x || !y || !layer || !weight || !isSeed || !clusterIndex))
+      return set_error(CLUE_EINVAL, "NULL input array");
+    const void* outs[10] = {out->x, out->y, out->z, out->eta, out->phi, out->r_over_absz, out->radius,
+                            out->layer, out->energy, out->isSilicon};
+    if (C > 0)
+      for (auto q : outs)
+        if (!q) return set_error(CLUE_EINVAL, "NULL output array");
+    Handle* h = reinterpret_cast<Handle*>(hh);
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    if ((rc = h->wait_previous())) return rc;
+    std::vector<size_t> need(clue::B_SLOTS, 0);
+    need[clue::B_OFF] = need[clue::B_COFF] = 8 * (size_t)(E + 1);
+    need[clue::B_COUNT] = 4 * (size_t)E;
+    need[clue::B_ACC] = 24 * (size_t)std::max<int64_t>(C, 1);
+    need[clue::B_SEED] = 4 * (size_t)std::max<int64_t>(C, 1);
+    need[clue::B_LZ] = 4 * (size_t)p->n_layers;
+    need[clue::B_FLAGS] = 4 * clue::kFlagCount;
+    if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
+    const size_t stage_bytes = 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers;
+    if ((rc = h->stage.reserve(stage_bytes))) return rc;
+    if ((rc = h->flags_host.reserve(4 * clue::kFlagCount))) return rc;
+    auto P = [&](int s) { return h->arena_bridge.ptr(s); };
+    char* st = static_cast<char*>(h->stage.p);
+    memcpy(st, off, 8 * (size_t)(E + 1));
+    memcpy(st + 8 * (size_t)(E + 1), coff, 8 * (size_t)(E + 1));
+    memcpy(st + 16 * (size_t)(E + 1), p->layer_z, 4 * (size_t)p->n_layers);
+    cudaStream_t s = h->stream;
+    if ((e = cudaMemcpyAsync(P(clue::B_OFF), st, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(P(clue::B_COFF), st + 8 * (size_t)(E + 1), 8 * (size_t)(E + 1), cudaMemcpyHostToDevice,
+                             s)) ||
+        (e = cudaMemcpyAsync(P(clue::B_LZ), st + 16 * (size_t)(E + 1), 4 * (size_t)p->n_layers,
+                             cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(P(clue::B_ACC), 0, 24 * (size_t)std::max<int64_t>(C, 1), s)) ||
+        (e = cudaMemsetAsync(P(clue::B_SEED), 0, 4 * (size_t)std::max<int64_t>(C, 1), s)) ||
+        (e = cudaMemsetAsync(P(clue::B_FLAGS), 0, 4 * clue::kFlagCount, s)))
+      return cuda_error(e, "bridge set-up");
+    int32_t* flags = static_cast<int32_t*>(P(clue::B_FLAGS));
+    auto* acc = static_cast<unsigned long long*>(P(clue::B_ACC));
+    auto* seed_of = static_cast<int32_t*>(P(clue::B_SEED));
+    if (N > 0)
+      clue::k_bridge_accumulate<<<clue::grid_for(N), 256, 0, s>>>(
+          E, N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int64_t*>(P(clue::B_COFF)), x, y,
+          weight, isSeed, clusterIndex, acc, seed_of, flags);
+    if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_accumulate");
+    if (C > 0)
+      clue::k_bridge_finalize<<<clue::grid_for(C), 256, 0, s>>>(C, acc, seed_of, x, y, layer,
+                                                                 static_cast<const float*>(P(clue::B_LZ)),
+                                                                 p->n_layers, p->radius, p->isSilicon, *out, flags);
+    if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_finalize");
+    if ((e = cudaMemcpyAsync(h->flags_host.p, flags, 4 * clue::kFlagCount, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return cuda_error(e, "bridge");
+    int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
+    const int32_t err = fh[clue::kFlagError];
+    fh[clue::kFlagError] = 0;
+    if (err == 1) return set_error(CLUE_EINVAL, "a clusterIndex is not below its event's cluster count");
+    if (err == 2) return set_error(CLUE_EINVAL, "a layer cluster's layer is outside [0, %d)", p->n_layers);
+    return CLUE_OK;
+  });
 }
 
 }  // extern "C"

@@ -682,37 +682,39 @@ extern "C" {
 const char* clue_last_error(void) { return clue::g_last_error.c_str(); }
 
 int clue_create(const clue_params* params, size_t budget, int device, void* stream, clue_handle** out) {
-  if (!params || !out) return set_error(CLUE_EINVAL, "NULL argument");
-  *out = nullptr;
-  int ndev = 0;
-  cudaError_t e = cudaGetDeviceCount(&ndev);
-  if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceCount");
-  if (device < 0 || device >= ndev) return set_error(CLUE_EINVAL, "device %d not present (%d devices)", device, ndev);
-  e = cudaSetDevice(device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  e = clue::prepare_clue2d_kernels(device);
-  if (e != cudaSuccess) return cuda_error(e, "preparing kernels");
-  Handle* h = new Handle();
-  h->device = device;
-  h->budget = budget ? budget : (size_t(16) << 30);
-  h->p2d = clue::make_params2d(params->dc, params->rhoc, params->outlierDeltaFactor);
-  if (stream) {
-    h->stream = static_cast<cudaStream_t>(stream);
-  } else {
-    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  return clue::guarded([&]() -> int {
+    if (!params || !out) return set_error(CLUE_EINVAL, "NULL argument");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return set_error(CLUE_EINVAL, "device %d not present (%d devices)", device, ndev);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    e = clue::prepare_clue2d_kernels(device);
+    if (e != cudaSuccess) return cuda_error(e, "preparing kernels");
+    Handle* h = new Handle();
+    h->device = device;
+    h->budget = budget ? budget : (size_t(16) << 30);
+    h->p2d = clue::make_params2d(params->dc, params->rhoc, params->outlierDeltaFactor);
+    if (stream) {
+      h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        delete h;
+        return cuda_error(e, "cudaStreamCreate");
+      }
+      h->owned_stream = h->stream;
+    }
+    e = cudaEventCreateWithFlags(&h->done_event, cudaEventDisableTiming);
     if (e != cudaSuccess) {
       delete h;
-      return cuda_error(e, "cudaStreamCreate");
+      return cuda_error(e, "cudaEventCreate");
     }
-    h->owned_stream = h->stream;
-  }
-  e = cudaEventCreateWithFlags(&h->done_event, cudaEventDisableTiming);
-  if (e != cudaSuccess) {
-    delete h;
-    return cuda_error(e, "cudaEventCreate");
-  }
-  *out = reinterpret_cast<clue_handle*>(h);
-  return CLUE_OK;
+    *out = reinterpret_cast<clue_handle*>(h);
+    return CLUE_OK;
+  });
 }
 
 int clue_destroy(clue_handle* hh) {
@@ -725,25 +727,27 @@ int clue_destroy(clue_handle* hh) {
 }
 
 int clue_set_stream(clue_handle* hh, void* stream) {
-  if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
-  Handle* h = reinterpret_cast<Handle*>(hh);
-  cudaError_t e = cudaSetDevice(h->device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  int rc = h->wait_previous();
-  if (rc) return rc;
-  if (stream) {
-    h->stream = static_cast<cudaStream_t>(stream);
-    return CLUE_OK;
-  }
-  if (!h->owned_stream) {
-    e = cudaStreamCreateWithFlags(&h->owned_stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
-      h->owned_stream = nullptr;
-      return cuda_error(e, "cudaStreamCreate");
+  return clue::guarded([&]() -> int {
+    if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
+    Handle* h = reinterpret_cast<Handle*>(hh);
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    int rc = h->wait_previous();
+    if (rc) return rc;
+    if (stream) {
+      h->stream = static_cast<cudaStream_t>(stream);
+      return CLUE_OK;
     }
-  }
-  h->stream = h->owned_stream;
-  return CLUE_OK;
+    if (!h->owned_stream) {
+      e = cudaStreamCreateWithFlags(&h->owned_stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        h->owned_stream = nullptr;
+        return cuda_error(e, "cudaStreamCreate");
+      }
+    }
+    h->stream = h->owned_stream;
+    return CLUE_OK;
+  });
 }
 
 int clue_set_params(clue_handle* hh, const clue_params* p) {
@@ -755,27 +759,33 @@ int clue_set_params(clue_handle* hh, const clue_params* p) {
 
 int clue_run_event(clue_handle* hh, int32_t n, const float* x, const float* y, const int32_t* layer,
                    const float* weight, const clue_outputs* out, int flags) {
-  if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
-  if (n < 0) return set_error(CLUE_EINVAL, "n < 0");
-  int64_t off[2] = {0, n};
-  return reinterpret_cast<Handle*>(hh)->run_batch(1, off, x, y, layer, weight, out, flags & ~CLUE_PLAIN);
+  return clue::guarded([&]() -> int {
+    if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
+    if (n < 0) return set_error(CLUE_EINVAL, "n < 0");
+    int64_t off[2] = {0, n};
+    return reinterpret_cast<Handle*>(hh)->run_batch(1, off, x, y, layer, weight, out, flags & ~CLUE_PLAIN);
+  });
 }
 
 int clue_run_batch(clue_handle* hh, int32_t n_events, const int64_t* event_offsets, const float* x, const float* y,
                    const int32_t* layer, const float* weight, const clue_outputs* out, int flags) {
-  if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
-  return reinterpret_cast<Handle*>(hh)->run_batch(n_events, event_offsets, x, y, layer, weight, out, flags);
+  return clue::guarded([&]() -> int {
+    if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
+    return reinterpret_cast<Handle*>(hh)->run_batch(n_events, event_offsets, x, y, layer, weight, out, flags);
+  });
 }
 
 int clue_synchronize(clue_handle* hh) {
-  if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
-  Handle* h = reinterpret_cast<Handle*>(hh);
-  cudaSetDevice(h->device);
-  int rc = h->wait_previous();
-  if (rc) return rc;
-  cudaError_t e = cudaStreamSynchronize(h->stream);
-  if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
-  return h->check_device_flags();
+  return clue::guarded([&]() -> int {
+    if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
+    Handle* h = reinterpret_cast<Handle*>(hh);
+    cudaSetDevice(h->device);
+    int rc = h->wait_previous();
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+    return h->check_device_flags();
+  });
 }
 
 size_t clue_required_bytes(int32_t n_events, int64_t n_points, int flags) {
@@ -787,8 +797,10 @@ size_t clue_required_bytes(int32_t n_events, int64_t n_points, int flags) {
 int clue_profile_batch(clue_handle* hh, int32_t n_events, const int64_t* event_offsets, const float* x,
                        const float* y, const int32_t* layer, const float* weight, const clue_outputs* out,
                        float* stage_ms) {
-  if (!hh || !out || !stage_ms) return set_error(CLUE_EINVAL, "NULL argument");
-  return reinterpret_cast<Handle*>(hh)->profile_batch(n_events, event_offsets, x, y, layer, weight, out, stage_ms);
+  return clue::guarded([&]() -> int {
+    if (!hh || !out || !stage_ms) return set_error(CLUE_EINVAL, "NULL argument");
+    return reinterpret_cast<Handle*>(hh)->profile_batch(n_events, event_offsets, x, y, layer, weight, out, stage_ms);
+  });
 }
 
 int clue_get_tuning(clue_handle* hh, clue_tuning* t) {

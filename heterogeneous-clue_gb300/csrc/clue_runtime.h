@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <exception>
+#include <new>
 #include <cstdint>
 #include <vector>
 
@@ -14,6 +16,21 @@ namespace clue {
 
 int set_error(int code, const char* fmt, ...);
 int cuda_error(cudaError_t e, const char* what);
+
+// Runs f() and turns a C++ exception into a status code: nothing may unwind
+// through the C ABI (a host allocation failing is CLUE_ENOMEM).
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return set_error(CLUE_ENOMEM, "host memory allocation failed");
+  } catch (const std::exception& e) {
+    return set_error(CLUE_EINVAL, "internal error: %s", e.what());
+  } catch (...) {
+    return set_error(CLUE_EINVAL, "internal error");
+  }
+}
 
 // Named, grow-only device buffers under a byte budget.  Buffers are only
 // reallocated when a request outgrows them, never per call.

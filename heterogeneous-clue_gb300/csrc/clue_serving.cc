@@ -63,7 +63,11 @@ void run_copies(const std::vector<CopyTask>& tasks) {
     for (size_t i; (i = next.fetch_add(1)) < pieces.size();) memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
   };
   std::vector<std::thread> th;
-  for (size_t k = 1; k < nth; ++k) th.emplace_back(work);
+  try {
+    for (size_t k = 1; k < nth; ++k) th.emplace_back(work);
+  } catch (...) {
+    // no more helper threads: the pieces left are copied by the ones running
+  }
   work();
   for (auto& t : th) t.join();
 }
@@ -453,16 +457,18 @@ using clue::set_error;
 extern "C" {
 
 int clue_server_create(const clue_params* params, const clue_server_config* cfg, clue_server** out) {
-  if (!params || !cfg || !out) return set_error(CLUE_EINVAL, "NULL argument");
-  *out = nullptr;
-  Server* s = new Server(*params, *cfg);
-  int rc = s->start();
-  if (rc) {
-    delete s;
-    return rc;
-  }
-  *out = reinterpret_cast<clue_server*>(s);
-  return CLUE_OK;
+  return clue::guarded([&]() -> int {
+    if (!params || !cfg || !out) return set_error(CLUE_EINVAL, "NULL argument");
+    *out = nullptr;
+    Server* s = new Server(*params, *cfg);
+    int rc = s->start();
+    if (rc) {
+      delete s;
+      return rc;
+    }
+    *out = reinterpret_cast<clue_server*>(s);
+    return CLUE_OK;
+  });
 }
 
 int clue_server_destroy(clue_server* s) {
@@ -472,31 +478,41 @@ int clue_server_destroy(clue_server* s) {
 
 int clue_server_submit(clue_server* s, int32_t n, const float* x, const float* y, const int32_t* layer,
                        const float* weight, const clue_outputs* out, int64_t* request_id) {
-  if (!s) return set_error(CLUE_EINVAL, "NULL server");
-  return reinterpret_cast<Server*>(s)->submit(n, x, y, layer, weight, out, request_id);
+  return clue::guarded([&]() -> int {
+    if (!s) return set_error(CLUE_EINVAL, "NULL server");
+    return reinterpret_cast<Server*>(s)->submit(n, x, y, layer, weight, out, request_id);
+  });
 }
 
 int clue_server_submit_many(clue_server* s, int32_t n_events, const int64_t* event_offsets, const float* x,
                             const float* y, const int32_t* layer, const float* weight, const clue_outputs* outs,
                             int64_t* request_ids) {
-  if (!s) return set_error(CLUE_EINVAL, "NULL server");
-  return reinterpret_cast<Server*>(s)->submit_many(n_events, event_offsets, x, y, layer, weight, outs, request_ids);
+  return clue::guarded([&]() -> int {
+    if (!s) return set_error(CLUE_EINVAL, "NULL server");
+    return reinterpret_cast<Server*>(s)->submit_many(n_events, event_offsets, x, y, layer, weight, outs, request_ids);
+  });
 }
 
 int clue_server_poll(clue_server* s, int64_t id, int32_t timeout_ms, double* latency_ms) {
-  if (!s) return set_error(CLUE_EINVAL, "NULL server");
-  return reinterpret_cast<Server*>(s)->poll(id, timeout_ms, latency_ms);
+  return clue::guarded([&]() -> int {
+    if (!s) return set_error(CLUE_EINVAL, "NULL server");
+    return reinterpret_cast<Server*>(s)->poll(id, timeout_ms, latency_ms);
+  });
 }
 
 int clue_server_drain(clue_server* s, int32_t timeout_ms) {
-  if (!s) return set_error(CLUE_EINVAL, "NULL server");
-  return reinterpret_cast<Server*>(s)->drain(timeout_ms);
+  return clue::guarded([&]() -> int {
+    if (!s) return set_error(CLUE_EINVAL, "NULL server");
+    return reinterpret_cast<Server*>(s)->drain(timeout_ms);
+  });
 }
 
 int clue_server_get_stats(clue_server* s, clue_server_stats* st) {
-  if (!s || !st) return set_error(CLUE_EINVAL, "NULL argument");
-  reinterpret_cast<Server*>(s)->stats(st);
-  return CLUE_OK;
+  return clue::guarded([&]() -> int {
+    if (!s || !st) return set_error(CLUE_EINVAL, "NULL argument");
+    reinterpret_cast<Server*>(s)->stats(st);
+    return CLUE_OK;
+  });
 }
 
 int clue_server_reset_stats(clue_server* s) {
