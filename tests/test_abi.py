@@ -19,10 +19,11 @@ def test_library_exports_every_declared_symbol(cuda_lib):
     assert not missing, f"declared in include/clue.h but not exported: {missing}"
 
 
-def test_library_is_native_sm103a_build():
-    # the shared object links CUDA code: it must mention the sm_103a fatbin section names via nvcc's registration
+def test_entry_points_have_c_linkage():
+    # plain (unmangled) text symbols: what cgo / JNI / ctypes / a C++ plugin bind to
     out = subprocess.run(["nm", "-D", "--defined-only", C.LIB_PATH], capture_output=True, text=True).stdout
-    assert " T clue_run_batch" in out and " T clue3d_run_batch" in out
+    for name in C.header_symbols():
+        assert f" T {name}\n" in out + "\n", name
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")
@@ -40,6 +41,14 @@ def test_null_arguments_are_einval(cuda_lib):
     assert cuda_lib.clue_run_batch(None, 0, None, None, None, None, None, None, 0) == C.CLUE_EINVAL
     assert "NULL" in C.last_error()
     assert cuda_lib.clue_destroy(None) == C.CLUE_OK
+    assert cuda_lib.clue_set_stream(None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_bridge_count(None, 0, None, None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_bridge_build(None, None, 0, None, None, None, None, None, None, None, None, None) == \
+        C.CLUE_EINVAL
+    assert cuda_lib.clue_server_submit_many(None, 0, None, None, None, None, None, None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_server_poll(None, 0, 0, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue3d_run_batch(None, None, 0, None, None, None, None, 0) == C.CLUE_EINVAL
+    assert cuda_lib.clue_run_event_noalloc(None, 0, None, None, None, None, None, None) == C.CLUE_EINVAL
 
 
 def test_required_bytes_grows_with_points(cuda_lib):
