@@ -107,6 +107,28 @@ def write_raw3d(path, events):
             f.write(rec.tobytes())
 
 
+def source_2d(path, max_events=-1):
+    """The event stream of the reference's Source2D (src/serial/bin/Source.cc:88-118,
+    147-186): a path containing "toyDetector" is one replicated cloud, replayed
+    10 times by default; any other file is raw2D, one cloud per event, each
+    once by default.  Events cycle through the clouds; ids start at 1.
+    Yields (event id, cloud)."""
+    toy = "toyDetector" in str(path)
+    clouds = [read_toy_detector(path)] if toy else read_raw2d(path)
+    n = max_events if max_events >= 0 else (10 if toy else len(clouds))
+    for i in range(n if clouds else 0):
+        yield i + 1, clouds[i % len(clouds)]
+
+
+def source_3d(path, max_events=-1):
+    """Source3D's stream (Source.cc:124-143,192-230): raw3D events, each once by
+    default, cycled; ids start at 1.  Yields (event id, ClusterCollection dict)."""
+    clouds = read_raw3d(path)
+    n = max_events if max_events >= 0 else len(clouds)
+    for i in range(n if clouds else 0):
+        yield i + 1, clouds[i % len(clouds)]
+
+
 def read_config(path):
     """A parameter file ``dc,rhoc,outlierDeltaFactor,produceOutput`` (one
     line, as config/hgcal_config.csv; parsed like src/serial/bin/main.cc:131-140:

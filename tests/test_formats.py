@@ -59,6 +59,26 @@ def test_raw3d_round_trip(tmp_path):
         assert np.array_equal(a["layer"], e["layer"]) and np.array_equal(a["isSilicon"], e["isSilicon"])
 
 
+def test_source_streams(tmp_path):
+    ev = S.toy_event(3, blobs_per_layer=1, noise_per_layer=3)
+    layer0 = {k: v[ev["layer"] == 0] for k, v in ev.items()}
+    toy = tmp_path / "toyDetector_1k.bin"
+    F.write_toy_detector(toy, layer0)
+    got = list(F.source_2d(toy))
+    assert [i for i, _ in got] == list(range(1, 11))  # ten replays of the one cloud by default
+    assert got[0][1]["x"].size == 100 * layer0["x"].size
+    assert len(list(F.source_2d(toy, max_events=3))) == 3
+    b = S.uneven_batch(3, seed=4, lo=1000, hi=2000)
+    raw = tmp_path / "raw2D.bin"
+    F.write_raw2d(raw, [S.event_of(b, e) for e in range(3)])
+    ids = [(i, c["x"].size) for i, c in F.source_2d(raw, max_events=5)]
+    sizes = [int(b["offsets"][e + 1] - b["offsets"][e]) for e in range(3)]
+    assert ids == [(1, sizes[0]), (2, sizes[1]), (3, sizes[2]), (4, sizes[0]), (5, sizes[1])]
+    r3 = tmp_path / "raw3D.bin"
+    F.write_raw3d(r3, [S.clue3d_event(1, n_clusters=50)])
+    assert [i for i, _ in F.source_3d(r3, max_events=2)] == [1, 2]
+
+
 def test_config_files(tmp_path):
     p = tmp_path / "hgcal_config.csv"
     p.write_text("1.3,0.11,2,0")
