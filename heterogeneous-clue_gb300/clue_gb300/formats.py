@@ -121,7 +121,7 @@ def source_2d(path, max_events=-1):
 
 
 def source_3d(path, max_events=-1):
-    """Source3D's stream (Source.cc:124-143,192-230): raw3D events, each once by
+    """Source3D's stream (Source.cc:124-143,190-226): raw3D events, each once by
     default, cycled; ids start at 1.  Yields (event id, ClusterCollection dict)."""
     clouds = read_raw3d(path)
     n = max_events if max_events >= 0 else len(clouds)
