@@ -189,7 +189,7 @@ def run_reference(args):
         evs += r["events"]
         pts += r["points"]
     v = evs / secs
-    sample = (f"{args.cpu_sample} events strided over the {args.events}-event workload "
+    sample = (f"{evs // max(args.steps, 1)} events strided over the {args.events}-event workload "
               f"({pts // max(args.steps, 1)} points) per step")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "events/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
