@@ -231,7 +231,7 @@ __device__ void order_queries(const LayerStore<TT, QT>& S, const int m, const fl
     const float2 p = rec_xy(S.rec[q]);
     const int bx0 = tile_bin(__fsub_rn(p.x, d)), bx1 = tile_bin(__fadd_rn(p.x, d));
     const int by0 = tile_bin(__fsub_rn(p.y, d)), by1 = tile_bin(__fadd_rn(p.y, d));
-    return NB - 1 - min(candidate_count(S.tbl, bx0, bx1, by0, by1) >> 2, NB - 1);
+    return NB - 1 - min(candidate_count(S.tbl, bx0, bx1, by0, by1) >> 1, NB - 1);  // 2 candidates per bucket
   };
   for (int i = tid; i < NB; i += NT) s_bins[i] = 0;
   __syncthreads();
