@@ -50,6 +50,7 @@ void DeviceArena::release() {
     b = Buf{};
   }
   total_ = 0;
+  ++gen_;
 }
 
 int DeviceArena::reserve(const std::vector<size_t>& need_in, size_t budget) {
@@ -87,6 +88,7 @@ int DeviceArena::reserve(const std::vector<size_t>& need_in, size_t budget) {
     bufs_[i].p = p;
     bufs_[i].bytes = bytes;
     total_ += bytes;
+    ++gen_;
   }
   return CLUE_OK;
 }
@@ -336,7 +338,8 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   }
   cudaError_t e;
   if (use_graph) {
-    GraphKey key{r.E, r.N, r.flags, h->tuning.threads, h->tuning.layer_capacity, h->tuning.ctas_per_sm,
+    GraphKey key{r.E, r.N, nchunks, h->arena.generation(), r.flags, h->tuning.threads, h->tuning.layer_capacity,
+                 h->tuning.ctas_per_sm,
                  h->tuning.big_threads, h->tuning.big_capacity,
                  h->tuning.work_tile_cm, h->p2d.dc, h->p2d.rhoc, h->p2d.odf,
                  {(const void*)r.x, (const void*)r.y, (const void*)r.layer, (const void*)r.w,

@@ -40,6 +40,7 @@ class DeviceArena {
   int reserve(const std::vector<size_t>& need, size_t budget);
   void* ptr(int slot) const { return slot < (int)bufs_.size() ? bufs_[slot].p : nullptr; }
   size_t total() const { return total_; }
+  uint64_t generation() const { return gen_; }  // bumped whenever a buffer is (re)allocated
   void release();
 
  private:
@@ -49,6 +50,7 @@ class DeviceArena {
   };
   std::vector<Buf> bufs_;
   size_t total_ = 0;
+  uint64_t gen_ = 0;
 };
 
 struct PinnedBuf {
@@ -62,13 +64,16 @@ struct PinnedBuf {
 struct GraphKey {
   int32_t E = -1;
   int64_t N = -1;
+  int64_t nchunks = -1;     // launch sizes of the chunk kernels are baked into the graph
+  uint64_t arena_gen = 0;   // and so are the addresses of every arena buffer
   int flags = 0;
   int threads = 0, cap = 0, ctas = 0, big_threads = 0, big_cap = 0;
   float work_tile = 0.f;
   float dc = 0.f, rhoc = 0.f, odf = 0.f;
   const void* ptrs[14] = {};
   bool operator==(const GraphKey& o) const {
-    if (E != o.E || N != o.N || flags != o.flags || threads != o.threads || cap != o.cap || ctas != o.ctas ||
+    if (E != o.E || N != o.N || nchunks != o.nchunks || arena_gen != o.arena_gen || flags != o.flags ||
+        threads != o.threads || cap != o.cap || ctas != o.ctas ||
         big_threads != o.big_threads || big_cap != o.big_cap ||
         work_tile != o.work_tile || dc != o.dc || rhoc != o.rhoc || odf != o.odf)
       return false;

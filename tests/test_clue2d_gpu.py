@@ -108,6 +108,24 @@ def test_device_memory_batch(algo, torch_cuda, extra):
     assert_bitexact(got, _oracle_batch(b))
 
 
+def test_graph_follows_new_event_boundaries(algo, torch_cuda):
+    """Same buffers, same event and point counts, other event boundaries (so
+    another number of chunks): the captured graph must not be replayed."""
+    torch = torch_cuda
+    b = S.uneven_batch(8, seed=17, lo=3000, hi=40000)
+    d = _to_dev(torch, b)
+    n = int(b["offsets"][-1])
+    out = _dev_out(torch, n)
+    off2 = b["offsets"].copy()
+    off2[1:-1] = np.sort(np.random.default_rng(3).choice(np.arange(1, n), off2.size - 2, replace=False))
+    for off in (b["offsets"], off2, b["offsets"]):
+        algo.run_batch(off, d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY)
+        algo.synchronize()
+        got = {k: v.cpu().numpy() for k, v in out.items()}
+        want = oracle.clue2d_batch(off, b["x"], b["y"], b["layer"], b["weight"], *PRM, n_threads=8)
+        assert_bitexact(got, want)
+
+
 def test_graph_replay_is_stable(algo):
     """The captured graph replays the same work: three calls, same outputs."""
     import torch
