@@ -84,7 +84,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-i", str(self.index), "-lms", "200"],
+                                          "-i", str(self.index), "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -406,26 +406,27 @@ def run_gb300(args):
     barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # clocks are sampled over the timed steps and the per-stage pass that follows
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
             run(0)
         ev1.record(stream)
         torch.cuda.synchronize()
-    algo.synchronize()
-    barrier()
+        algo.synchronize()
+        barrier()
+
+        # ---- per-stage times of the same workload (roofline of the dominant kernel)
+        stage_sum = {s: 0.0 for s in C.STAGES}
+        prof_steps = max(1, min(args.steps, 5))
+        for _ in range(prof_steps):
+            st = algo.profile_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out)
+            for k, v in st.items():
+                stage_sum[k] += v
     ms = max_over_ranks(ev0.elapsed_time(ev1))
     ms_step = ms / args.steps
     value = ws * E * args.steps / (ms / 1000.0)
     gpts = ws * N * args.steps / (ms / 1000.0) / 1e9
-
-    # ---- per-stage times of the same workload (roofline of the dominant kernel)
-    stage_sum = {s: 0.0 for s in C.STAGES}
-    prof_steps = max(1, min(args.steps, 5))
-    for _ in range(prof_steps):
-        st = algo.profile_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out)
-        for k, v in st.items():
-            stage_sum[k] += v
     stage_ms = {k: v / prof_steps for k, v in stage_sum.items()}
     peak, peak_kind = _peak_hbm()
     layers_ms = stage_ms["layers"]
