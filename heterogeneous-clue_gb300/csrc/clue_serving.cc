@@ -90,7 +90,8 @@ struct Slot {
   std::vector<Request*> reqs;
   bool busy = false;      // requests taken (staging, on the device or delivering results)
   bool launched = false;  // the batch is queued on the device
-  int64_t cap_points = 0;
+  int64_t cap_points = 0;    // largest batch the slot's share of the budget holds
+  int64_t batch_points = 0;  // batches are cut at this size: the buffers sized at start
 };
 
 class Server {
@@ -121,6 +122,7 @@ class Server {
       // resident buffers for batches up to 8M points, so that ordinary loads
       // never allocate (and never synchronise the device) on the serving path
       const int64_t pre = std::min<int64_t>(s.cap_points, int64_t(8) << 20);
+      s.batch_points = pre;
       cudaSetDevice(cfg_.device);
       rc = reserve_2d(hh, cfg_.max_batch_events, pre, true);
       if (!rc) rc = s.in.reserve(16 * (size_t)pre);
@@ -338,7 +340,9 @@ class Server {
     int64_t pts = 0;
     while (!queue_.empty() && (int)s.reqs.size() < cfg_.max_batch_events) {
       Request* r = queue_.front();
-      if (pts + r->n > s.cap_points && !s.reqs.empty()) break;
+      // batches stay within the buffers sized at start (a single larger event
+      // still goes, alone, and grows them once)
+      if (pts + r->n > s.batch_points && !s.reqs.empty()) break;
       queue_.pop_front();
       s.reqs.push_back(r);
       pts += r->n;
