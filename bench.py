@@ -42,7 +42,7 @@ METRIC = "CLUE events/s & Gpoints/s, batched vs plain on 1 GB300 (bit-exact); p9
 BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
-STAGES_PER_STEP = 8   # kernels of one batch, plus the large-layer pass when the tuning has one
+STAGES_PER_STEP = 9   # kernels of one batch, plus the large-layer pass when the tuning has one
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
@@ -494,8 +494,9 @@ def run_gb300(args):
         for _ in range(args.steps):
             algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
         dt = max_over_ranks(time.perf_counter() - t0)
+        h2d_bytes, d2h_bytes = algo.last_transfer()  # as the library copied them
         e2e = {"value": ws * E * args.steps / dt, "unit": "events/s",
-               "h2d_bytes_per_step": 16 * N + 12 * (E + 1), "d2h_bytes_per_step": 20 * N + 32,
+               "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps}
         del hin, hout
 

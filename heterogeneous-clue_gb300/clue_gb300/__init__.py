@@ -128,6 +128,7 @@ def lib():
         "clue_run_batch": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), ctypes.c_int],
                            ctypes.c_int),
         "clue_synchronize": ([H], ctypes.c_int),
+        "clue_last_transfer": ([H, _i64p, _i64p], ctypes.c_int),
         "clue_required_bytes": ([ctypes.c_int32, ctypes.c_int64, ctypes.c_int], ctypes.c_size_t),
         "clue_get_tuning": ([H, ctypes.POINTER(Tuning)], ctypes.c_int),
         "clue_profile_batch": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), _f32p],
@@ -263,6 +264,12 @@ class Clusterizer:
         check(lib().clue_profile_batch(self._h, offsets.size - 1, offsets.ctypes.data_as(_i64p), _ptr(x), _ptr(y),
                                        _ptr(layer), _ptr(weight), ctypes.byref(os_), ms.ctypes.data_as(_f32p)))
         return dict(zip(STAGES, ms.tolist()))
+
+    def last_transfer(self):
+        """(h2d_bytes, d2h_bytes) the last 2D run on this handle copied."""
+        a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+        check(lib().clue_last_transfer(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def synchronize(self):
         check(lib().clue_synchronize(self._h))

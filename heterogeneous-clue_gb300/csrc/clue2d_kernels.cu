@@ -537,6 +537,9 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
   __shared__ int s_e;
   __shared__ int s_cnt[kLayers];
   for (int l = threadIdx.x; l < kLayers; l += kChunkThreads) s_cnt[l] = 0;
+  // the size histogram of k_layer_scan starts from zero (it runs after this kernel)
+  if (c == 0)
+    for (int i = threadIdx.x; i < 2 * kSizeBuckets; i += kChunkThreads) b.size_hist[i] = 0;
   if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
   __syncthreads();
   const int e = s_e;
@@ -587,7 +590,11 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
     if (s_cnt[l]) atomicAdd(&b.lcnt[e * kLayers + l], s_cnt[l]);
 }
 
-// One warp per event: layers 4*lane .. 4*lane+3.
+// Size class of a non-empty layer: 0 for the largest.
+__device__ __forceinline__ int size_bucket(int m) { return kSizeBuckets - 1 - min(m >> 4, kSizeBuckets - 1); }
+
+// One warp per event: layers 4*lane .. 4*lane+3.  Also counts the non-empty
+// layers per size class for k_order.
 __global__ void k_layer_scan(Batch2D b) {
   const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (e >= b.n_events) return;
@@ -615,6 +622,43 @@ __global__ void k_layer_scan(Batch2D b) {
       b.cursor[e * kLayers + l] = run;
     }
     run += c[j];
+    const int key = c[j] > 0 ? size_bucket(c[j]) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(&b.size_hist[key], __popc(grp));
+  }
+}
+
+// The non-empty (event, layer) items in descending size class (a counting
+// sort over the classes; the order inside a class is arbitrary).  The layer
+// kernel takes its tickets in this order, so each pass ends on its smallest
+// layers instead of on whichever layer came last.  Which CTA runs which
+// layer never changes a result.  One warp per event; 256 threads per block,
+// one per size class for the scan.
+__global__ void __launch_bounds__(kSizeBuckets) k_order(Batch2D b) {
+  static_assert(kSizeBuckets == 256, "one thread per size class");
+  __shared__ int s_base[kSizeBuckets];
+  __shared__ int s_ws[33];
+  const int tid = threadIdx.x;
+  const int v = b.size_hist[tid];
+  int total;
+  const int inc = block_inclusive_scan<kSizeBuckets>(v, s_ws, &total);
+  s_base[tid] = inc - v;
+  if (blockIdx.x == 0 && tid == 0) b.flags[kFlagOrdered] = total;
+  __syncthreads();
+  const int e = (blockIdx.x * blockDim.x + tid) >> 5;
+  if (e >= b.n_events) return;
+  const int lane = lane_id();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int l0 = 0; l0 < kLayers; l0 += 32) {
+    const int l = l0 + lane;
+    const int m = l < kLayers ? b.lcnt[e * kLayers + l] : 0;
+    const int key = m > 0 ? size_bucket(m) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(grp) - 1;
+    int pos = 0;
+    if (key >= 0 && lane == leader) pos = atomicAdd(&b.size_hist[kSizeBuckets + key], __popc(grp));
+    pos = __shfl_sync(0xffffffffu, pos, leader);
+    if (key >= 0) b.order[s_base[key] + pos + __popc(grp & lt)] = e * kLayers + l;
   }
 }
 
@@ -650,7 +694,8 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
   }
 }
 
-// Persistent CTAs over the (event, layer) queue.  Two classes of layers: the
+// Persistent CTAs over the (event, layer) queue, largest layers first (k_order).
+// Two classes of layers: the
 // first pass (big_pass = 0) takes every item from an atomic ticket and
 // handles layers of at most max_m points on chip with `cap` points of shared
 // memory (several CTAs per SM); larger layers are appended to a list that the
@@ -663,7 +708,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   __shared__ int s_next;
   __shared__ int s_ws[33];
   __shared__ int s_bins[64];
-  const int n_items = b.n_events * kLayers;
+  const int n_ordered = b.flags[kFlagOrdered];
   const bool grouped = b.flags[kFlagGrouped] != 0;
   LayerStore<uint16_t, uint16_t> sm;
   sm.tbl = reinterpret_cast<uint16_t*>(dsm);
@@ -677,7 +722,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   auto fetch = [&]() {
     if (!big_pass) {
       const int t = atomicAdd(&b.flags[kFlagTicket], 1);
-      return t < n_items ? t : -1;
+      return t < n_ordered ? b.order[t] : -1;
     }
     const int t = atomicAdd(&b.flags[kFlagTicket2], 1);
     return t < b.flags[kFlagBigCount] ? big_list[t] : -1;
@@ -967,6 +1012,7 @@ cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t
   k_count<<<nc, kChunkThreads, 0, s>>>(b);
   mark(1);
   k_layer_scan<<<warps_grid, 256, 0, s>>>(b);
+  k_order<<<warps_grid, kSizeBuckets, 0, s>>>(b);
   mark(2);
   k_scatter<<<nc, kChunkThreads, 0, s>>>(b);
   err = cudaGetLastError();

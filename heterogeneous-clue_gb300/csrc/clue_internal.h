@@ -21,6 +21,8 @@ constexpr int kTableStride = ((kTableInts * 4 + 15) / 16) * 4;
 // Points per event-aligned chunk of the streaming kernels (count, scatter, seed ranks).
 constexpr int kChunk = 4096;
 constexpr int kChunkThreads = 512;
+// Size classes of the largest-first layer order (16 points per class).
+constexpr int kSizeBuckets = 256;
 
 // Device-side status words of one run.
 enum FlagSlot : int {
@@ -30,6 +32,7 @@ enum FlagSlot : int {
   kFlagSpilled = 3,
   kFlagTicket2 = 4,   // ticket of the large-layer pass
   kFlagBigCount = 5,  // layers left to the large-layer pass
+  kFlagOrdered = 6,   // non-empty layers in the size order
   kFlagCount = 8
 };
 
@@ -76,6 +79,8 @@ struct Batch2D {
   int32_t* lcnt = nullptr;    // [E*100] points per (event, layer)
   int32_t* lstart = nullptr;  // [E*100] first grouped position of (event, layer)
   int32_t* cursor = nullptr;  // [E*100]
+  int32_t* order = nullptr;      // [E*100] non-empty (event, layer) items, largest first
+  int32_t* size_hist = nullptr;  // [2*kSizeBuckets] layers per size class, then cursors
   float* gx = nullptr;        // [N] grouped copies, event-local index in gid
   float* gy = nullptr;
   float* gw = nullptr;

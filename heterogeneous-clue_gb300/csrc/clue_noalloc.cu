@@ -43,7 +43,8 @@ constexpr size_t kOffChunkStart = kOffOffsets + al(16);                        /
 constexpr size_t kOffLcnt = kOffChunkStart + al(8);                            // int32[100]
 constexpr size_t kOffLstart = kOffLcnt + al(4 * kLayers);                      // int32[100]
 constexpr size_t kOffCursor = kOffLstart + al(4 * kLayers);                    // int32[100]
-constexpr size_t kOffFlags = kOffCursor + al(4 * kLayers);                     // int32[kFlagCount]
+constexpr size_t kOffOrder = kOffCursor + al(4 * kLayers);                     // int32[100 + 2 * size classes]
+constexpr size_t kOffFlags = kOffOrder + al(4 * (kLayers + 2 * kSizeBuckets));  // int32[kFlagCount]
 constexpr size_t kOffChunkSeeds = kOffFlags + al(4 * kFlagCount);              // int32[chunks]
 constexpr size_t kOffChunkBase = kOffChunkSeeds + al(4 * kNoAllocMaxChunks);   // int32[chunks]
 constexpr size_t kOffGx = kOffChunkBase + al(4 * kNoAllocMaxChunks);           // 4 x [N] grouped copies
@@ -127,6 +128,8 @@ extern "C" int clue_run_event_noalloc(const clue_params* params, int32_t n, cons
   b.lstart = reinterpret_cast<int32_t*>(base + kOffLstart);
   b.cursor = reinterpret_cast<int32_t*>(base + kOffCursor);
   b.flags = reinterpret_cast<int32_t*>(base + kOffFlags);
+  b.order = reinterpret_cast<int32_t*>(base + kOffOrder);
+  b.size_hist = b.order + kLayers;
   b.chunk_seeds = reinterpret_cast<int32_t*>(base + kOffChunkSeeds);
   b.chunk_base = reinterpret_cast<int32_t*>(base + kOffChunkBase);
   const size_t plane = al(4 * kNoAllocMaxPoints);

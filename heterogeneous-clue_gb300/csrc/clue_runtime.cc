@@ -116,7 +116,7 @@ namespace {
 enum Slot2D : int {
   S_OFF, S_CS, S_LCNT, S_LSTART, S_CURSOR, S_GX, S_GY, S_GW, S_GID,
   S_SP0, S_SP1, S_SP2, S_SP3, S_SP4, S_SP5, S_SP6, S_SP7,
-  S_SPTBL, S_CSEED, S_CBASE, S_FLAGS,
+  S_SPTBL, S_CSEED, S_CBASE, S_FLAGS, S_ORDER,
   S_IN_X, S_IN_Y, S_IN_L, S_IN_W, S_OUT_RHO, S_OUT_DELTA, S_OUT_NH, S_OUT_SEED, S_OUT_CI,
   S_COUNT
 };
@@ -140,6 +140,7 @@ std::vector<size_t> sizes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bo
   s[S_SPTBL] = 4 * (size_t)kTableStride * grid;
   s[S_CSEED] = s[S_CBASE] = 4 * (size_t)std::max<int64_t>(nchunks, 1);
   s[S_FLAGS] = 4 * kFlagCount;
+  s[S_ORDER] = 4 * ((size_t)E * kLayers + 2 * kSizeBuckets);
   if (host_io) {
     s[S_IN_X] = s[S_IN_Y] = s[S_IN_L] = s[S_IN_W] = 4 * (size_t)N;
     s[S_OUT_RHO] = s[S_OUT_DELTA] = s[S_OUT_NH] = s[S_OUT_SEED] = s[S_OUT_CI] = 4 * (size_t)N;
@@ -304,6 +305,8 @@ void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, 
   b.chunk_seeds = static_cast<int32_t*>(P(S_CSEED));
   b.chunk_base = static_cast<int32_t*>(P(S_CBASE));
   b.flags = static_cast<int32_t*>(P(S_FLAGS));
+  b.order = static_cast<int32_t*>(P(S_ORDER));
+  b.size_hist = b.order + (size_t)r.E * kLayers;
 }
 
 int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullptr) {
@@ -380,6 +383,8 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
   h->error_layers = kLayers;
+  h->last_h2d = 12 * (int64_t)(r.E + 1) + (host_io ? 16 * r.N : 0);
+  h->last_d2h = 4 * kFlagCount + (host_io ? 20 * r.N : 0);
   if (host_io && !(r.flags & kAsyncHostIO)) {
     rc = h->wait_previous();
     if (rc) return rc;
@@ -425,6 +430,8 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   e = cudaMemcpyAsync(h->arena.ptr(S_CS), sc, 8 * (size_t)r.E, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "H2D chunk table");
   int any_error = 0;
+  h->last_h2d = 24 * (int64_t)r.E + (host_io ? 16 * r.N : 0);
+  h->last_d2h = 0;
   for (int32_t ev = 0; ev < r.E; ++ev) {
     const int64_t s0 = r.off[ev], n = r.off[ev + 1] - s0;
     if (n == 0) continue;
@@ -477,6 +484,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) return cuda_error(e, "per-event synchronise");
       any_error |= static_cast<int32_t*>(h->flags_host.p)[kFlagError];
+      h->last_d2h += 20 * n + 4 * kFlagCount;
     }
   }
   if (host_io) {
@@ -487,6 +495,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   // never clears it) and is read back at clue_synchronize.
   e = cudaMemcpyAsync(h->flags_host.p, h->arena.ptr(S_FLAGS), 4 * kFlagCount, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_error(e, "D2H status");
+  h->last_d2h = 4 * kFlagCount;
   e = cudaEventRecord(h->done_event, s);
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
@@ -608,6 +617,8 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaEventRecord(d2h[k], co)) != cudaSuccess)
       return cuda_error(e, "D2H sub-batch");
   }
+  h->last_h2d = 16 * r.N + 12 * (int64_t)(r.E + S);
+  h->last_d2h = 20 * r.N + 4 * kFlagCount * (int64_t)S;
   // the handle's stream orders after the last copy-out, so later work and
   // clue_synchronize see a finished batch
   for (int k = 0; k < kPipeSlots; ++k)
@@ -776,6 +787,14 @@ int clue_run_batch(clue_handle* hh, int32_t n_events, const int64_t* event_offse
     if (!hh) return set_error(CLUE_EINVAL, "NULL handle");
     return reinterpret_cast<Handle*>(hh)->run_batch(n_events, event_offsets, x, y, layer, weight, out, flags);
   });
+}
+
+int clue_last_transfer(clue_handle* hh, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+  if (!hh || !h2d_bytes || !d2h_bytes) return set_error(CLUE_EINVAL, "NULL argument");
+  const Handle* h = reinterpret_cast<const Handle*>(hh);
+  *h2d_bytes = h->last_h2d;
+  *d2h_bytes = h->last_d2h;
+  return CLUE_OK;
 }
 
 int clue_synchronize(clue_handle* hh) {

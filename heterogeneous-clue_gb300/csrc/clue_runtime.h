@@ -114,6 +114,7 @@ struct Handle {
   cudaStream_t copy_in = nullptr;         // pipelined host-memory path: H2D stream
   cudaStream_t copy_out = nullptr;        // and D2H stream
   cudaEvent_t pipe_events[3 * kPipeSlots] = {};  // per slot: H2D done, kernels done, D2H done
+  int64_t last_h2d = 0, last_d2h = 0;     // host<->device bytes of the last 2D run
   PinnedBuf stage;
   PinnedBuf flags_host;
   PinnedBuf nt_host;

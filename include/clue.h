@@ -104,6 +104,11 @@ int clue_run_batch(clue_handle* h, int32_t n_events, const int64_t* event_offset
  * error recorded on the device (e.g. a layer outside [0, 100)). */
 int clue_synchronize(clue_handle* h);
 
+/* Host<->device bytes the last CLUE 2D run on this handle copied (points,
+ * outputs, offset and chunk tables, status words; device-memory runs copy
+ * only the tables and the status). */
+int clue_last_transfer(clue_handle* h, int64_t* h2d_bytes, int64_t* d2h_bytes);
+
 /* Device bytes a batch of n_points points in n_events events needs. */
 size_t clue_required_bytes(int32_t n_events, int64_t n_points, int flags);
 

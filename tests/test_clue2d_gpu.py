@@ -266,7 +266,11 @@ def test_host_memory_pipelined_large_batch(algo):
     n = int(b["offsets"][-1])
     assert n >= 32 << 20  # four or more sub-batches
     got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
+    h2d, d2h = algo.last_transfer()
+    assert 16 * n < h2d < 16 * n + 64 * b["offsets"].size
+    assert 20 * n < d2h < 20 * n + 4096  # outputs plus one status block per sub-batch
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
+    assert algo.last_transfer() == (16 * n + 12 * b["offsets"].size, 20 * n + 32)
     assert_bitexact(got, ref)
     for e in (0, 359, 759):
         s, t = b["offsets"][e], b["offsets"][e + 1]
