@@ -42,7 +42,6 @@ METRIC = "CLUE events/s & Gpoints/s, batched vs plain on 1 GB300 (bit-exact); p9
 BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
-STAGES_PER_STEP = 9   # kernels of one batch, plus the large-layer pass when the tuning has one
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
@@ -395,13 +394,11 @@ def run_gb300(args):
     def run(flags):
         algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
 
-    t_now = algo.get_tuning()
-    launches_per_step = STAGES_PER_STEP + (1 if t_now["big_threads"] > 0 and
-                                           t_now["big_capacity"] > t_now["layer_capacity"] else 0)
-
     # ---- batched, device resident (headline value)
     for _ in range(args.warmup):
         run(0)
+    # kernels per step as the library counted them (the graph's kernels)
+    launches_per_step = algo.last_run_stats()["kernel_launches"]
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
@@ -494,7 +491,8 @@ def run_gb300(args):
         for _ in range(args.steps):
             algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
         dt = max_over_ranks(time.perf_counter() - t0)
-        h2d_bytes, d2h_bytes = algo.last_transfer()  # as the library copied them
+        st = algo.last_run_stats()  # the copies as the library made them
+        h2d_bytes, d2h_bytes = st["h2d_bytes"], st["d2h_bytes"]
         e2e = {"value": ws * E * args.steps / dt, "unit": "events/s",
                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps}

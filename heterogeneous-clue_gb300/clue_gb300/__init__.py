@@ -92,6 +92,10 @@ class ServerConfig(ctypes.Structure):
                 ("max_batch_events", ctypes.c_int32), ("device", ctypes.c_int32)]
 
 
+class RunStats(ctypes.Structure):
+    _fields_ = [("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_int64), ("batches", ctypes.c_int64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("mean_batch_events", ctypes.c_double),
@@ -128,7 +132,7 @@ def lib():
         "clue_run_batch": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), ctypes.c_int],
                            ctypes.c_int),
         "clue_synchronize": ([H], ctypes.c_int),
-        "clue_last_transfer": ([H, _i64p, _i64p], ctypes.c_int),
+        "clue_last_run_stats": ([H, ctypes.POINTER(RunStats)], ctypes.c_int),
         "clue_required_bytes": ([ctypes.c_int32, ctypes.c_int64, ctypes.c_int], ctypes.c_size_t),
         "clue_get_tuning": ([H, ctypes.POINTER(Tuning)], ctypes.c_int),
         "clue_profile_batch": ([H, ctypes.c_int32, _i64p, _vp, _vp, _vp, _vp, ctypes.POINTER(Outputs), _f32p],
@@ -265,11 +269,12 @@ class Clusterizer:
                                        _ptr(layer), _ptr(weight), ctypes.byref(os_), ms.ctypes.data_as(_f32p)))
         return dict(zip(STAGES, ms.tolist()))
 
-    def last_transfer(self):
-        """(h2d_bytes, d2h_bytes) the last 2D run on this handle copied."""
-        a, b = ctypes.c_int64(0), ctypes.c_int64(0)
-        check(lib().clue_last_transfer(self._h, ctypes.byref(a), ctypes.byref(b)))
-        return a.value, b.value
+    def last_run_stats(self):
+        """Copies and kernels of the last 2D run on this handle:
+        {"h2d_bytes", "d2h_bytes", "kernel_launches"}."""
+        st = RunStats()
+        check(lib().clue_last_run_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in RunStats._fields_}
 
     def synchronize(self):
         check(lib().clue_synchronize(self._h))

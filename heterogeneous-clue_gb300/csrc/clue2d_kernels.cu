@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
   __shared__ int s_cnt[kLayers];
   for (int l = threadIdx.x; l < kLayers; l += kChunkThreads) s_cnt[l] = 0;
   // the size histogram of k_layer_scan starts from zero (it runs after this kernel)
-  if (c == 0)
+  if (c == 0 && b.use_order)
     for (int i = threadIdx.x; i < 2 * kSizeBuckets; i += kChunkThreads) b.size_hist[i] = 0;
   if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
   __syncthreads();
@@ -622,6 +622,7 @@ __global__ void k_layer_scan(Batch2D b) {
       b.cursor[e * kLayers + l] = run;
     }
     run += c[j];
+    if (!b.use_order) continue;
     const int key = c[j] > 0 ? size_bucket(c[j]) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, key);
     if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(&b.size_hist[key], __popc(grp));
@@ -694,8 +695,8 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
   }
 }
 
-// Persistent CTAs over the (event, layer) queue, largest layers first (k_order).
-// Two classes of layers: the
+// Persistent CTAs over the (event, layer) queue, in event order or, when
+// launched with use_order, largest layers first (k_order).  Two classes of layers: the
 // first pass (big_pass = 0) takes every item from an atomic ticket and
 // handles layers of at most max_m points on chip with `cap` points of shared
 // memory (several CTAs per SM); larger layers are appended to a list that the
@@ -708,7 +709,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   __shared__ int s_next;
   __shared__ int s_ws[33];
   __shared__ int s_bins[64];
-  const int n_ordered = b.flags[kFlagOrdered];
+  const int n_items = b.use_order ? b.flags[kFlagOrdered] : b.n_events * kLayers;
   const bool grouped = b.flags[kFlagGrouped] != 0;
   LayerStore<uint16_t, uint16_t> sm;
   sm.tbl = reinterpret_cast<uint16_t*>(dsm);
@@ -722,7 +723,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
   auto fetch = [&]() {
     if (!big_pass) {
       const int t = atomicAdd(&b.flags[kFlagTicket], 1);
-      return t < n_ordered ? b.order[t] : -1;
+      if (t >= n_items) return -1;
+      return b.use_order ? b.order[t] : t;
     }
     const int t = atomicAdd(&b.flags[kFlagTicket2], 1);
     return t < b.flags[kFlagBigCount] ? big_list[t] : -1;
@@ -988,9 +990,19 @@ int layer_grid(const Tuning2D& t, int n_items) {
   return g < 1 ? 1 : g;
 }
 
-cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s,
-                          cudaEvent_t* ev) {
-  if (b.n_events <= 0 || b.n_points <= 0) return cudaSuccess;
+cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2D& t, cudaStream_t s,
+                          cudaEvent_t* ev, int64_t* kernels) {
+  if (batch.n_events <= 0 || batch.n_points <= 0) return cudaSuccess;
+  // Largest layers first only where a pass ends on a visible tail: a few
+  // layers per CTA (a sub-batch, a served batch).  With one layer per CTA or
+  // less (a single event) every layer starts at once, and with hundreds per
+  // CTA the tail is negligible and the event order measured faster.
+  Batch2D b = batch;
+  {
+    const int n_items = b.n_events * kLayers;
+    const int g = layer_grid(t, n_items);
+    b.use_order = (n_items > g && n_items <= 64 * g) ? 1 : 0;
+  }
   cudaError_t err;
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
@@ -1012,15 +1024,15 @@ cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t
   k_count<<<nc, kChunkThreads, 0, s>>>(b);
   mark(1);
   k_layer_scan<<<warps_grid, 256, 0, s>>>(b);
-  k_order<<<warps_grid, kSizeBuckets, 0, s>>>(b);
+  if (b.use_order) k_order<<<warps_grid, kSizeBuckets, 0, s>>>(b);
   mark(2);
   k_scatter<<<nc, kChunkThreads, 0, s>>>(b);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   mark(3);
+  const bool two_class = t.big_threads > 0 && t.big_capacity > t.layer_capacity;
   {
     const int n_items = b.n_events * kLayers;
-    const bool two_class = t.big_threads > 0 && t.big_capacity > t.layer_capacity;
     err = launch_layers_any(t.threads, b, p, t.layer_capacity, two_class ? t.layer_capacity : INT_MAX, 0,
                             layer_grid(t, n_items), s);
     if (err == cudaSuccess && two_class) {
@@ -1040,6 +1052,7 @@ cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t
   mark(7);
   k_label<<<nc, kChunkThreads, 0, s>>>(b);
   mark(8);
+  if (kernels) *kernels += 8 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -79,6 +79,7 @@ struct Batch2D {
   int32_t* lcnt = nullptr;    // [E*100] points per (event, layer)
   int32_t* lstart = nullptr;  // [E*100] first grouped position of (event, layer)
   int32_t* cursor = nullptr;  // [E*100]
+  int32_t use_order = 0;         // set per launch: take the layers in `order`
   int32_t* order = nullptr;      // [E*100] non-empty (event, layer) items, largest first
   int32_t* size_hist = nullptr;  // [2*kSizeBuckets] layers per size class, then cursors
   float* gx = nullptr;        // [N] grouped copies, event-local index in gid
@@ -104,9 +105,10 @@ cudaError_t prepare_clue2d_kernels(int device);
 
 constexpr int kStages2D = 8;
 // Queues the whole 2D pipeline of one batch on `s`.  With `stage_events`
-// (kStages2D + 1 events) an event is recorded before each stage and after the last.
+// (kStages2D + 1 events) an event is recorded before each stage and after the
+// last; `kernels`, when given, is increased by the number of kernels queued.
 cudaError_t launch_clue2d(const Batch2D& b, const Params2D& p, const Tuning2D& t, cudaStream_t s,
-                          cudaEvent_t* stage_events = nullptr);
+                          cudaEvent_t* stage_events = nullptr, int64_t* kernels = nullptr);
 
 // Adds an order-sensitive digest of n_words 32-bit words to *d_out.
 cudaError_t launch_digest(const void* words, int64_t n_words, unsigned long long* d_out, cudaStream_t s);

@@ -229,7 +229,8 @@ int validate_offsets(int32_t E, const int64_t* off) {
 }
 
 // Queues the batch pipeline (copies included in host mode) on h->stream.
-int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t* stage_events = nullptr) {
+int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t* stage_events = nullptr,
+               int64_t* kernels = nullptr) {
   cudaStream_t s = h->stream;
   cudaError_t e;
   const size_t n4 = 4 * (size_t)r.N;
@@ -247,7 +248,7 @@ int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t*
         (e = cudaMemcpyAsync((void*)b.w, r.w, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_error(e, "H2D points");
   }
-  e = launch_clue2d(b, h->p2d, h->tuning, s, stage_events);
+  e = launch_clue2d(b, h->p2d, h->tuning, s, stage_events, kernels);
   if (e != cudaSuccess) return cuda_error(e, "launching CLUE kernels");
   if (host_io) {
     const clue_outputs* o = r.out;
@@ -340,6 +341,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
                 is_pinned_or_device(r.out->isSeed) && is_pinned_or_device(r.out->clusterIndex);
   }
   cudaError_t e;
+  int64_t kernels = 0;
   if (use_graph) {
     GraphKey key{r.E, r.N, nchunks, h->arena.generation(), r.flags, h->tuning.threads, h->tuning.layer_capacity,
                  h->tuning.ctas_per_sm,
@@ -357,11 +359,12 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
       cudaStream_t s = h->stream;
       e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return cuda_error(e, "cudaStreamBeginCapture");
-      rc = enqueue_2d(h, r, b, host_io);
+      rc = enqueue_2d(h, r, b, host_io, nullptr, &h->graph_kernels);
       cudaGraph_t g = nullptr;
       cudaError_t e2 = cudaStreamEndCapture(s, &g);
       if (rc) {
         if (g) cudaGraphDestroy(g);
+        h->graph_kernels = 0;
         return rc;
       }
       if (e2 != cudaSuccess) return cuda_error(e2, "cudaStreamEndCapture");
@@ -375,16 +378,18 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
     }
     e = cudaGraphLaunch(h->graph_exec, h->stream);
     if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+    kernels = h->graph_kernels;
   } else {
-    rc = enqueue_2d(h, r, b, host_io, stage_events);
+    rc = enqueue_2d(h, r, b, host_io, stage_events, &kernels);
     if (rc) return rc;
   }
   e = cudaEventRecord(h->done_event, h->stream);
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
   h->error_layers = kLayers;
-  h->last_h2d = 12 * (int64_t)(r.E + 1) + (host_io ? 16 * r.N : 0);
-  h->last_d2h = 4 * kFlagCount + (host_io ? 20 * r.N : 0);
+  h->last_run.h2d_bytes = 12 * (int64_t)(r.E + 1) + (host_io ? 16 * r.N : 0);
+  h->last_run.d2h_bytes = 4 * kFlagCount + (host_io ? 20 * r.N : 0);
+  h->last_run.kernel_launches = kernels;
   if (host_io && !(r.flags & kAsyncHostIO)) {
     rc = h->wait_previous();
     if (rc) return rc;
@@ -430,8 +435,9 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   e = cudaMemcpyAsync(h->arena.ptr(S_CS), sc, 8 * (size_t)r.E, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "H2D chunk table");
   int any_error = 0;
-  h->last_h2d = 24 * (int64_t)r.E + (host_io ? 16 * r.N : 0);
-  h->last_d2h = 0;
+  h->last_run.h2d_bytes = 24 * (int64_t)r.E + (host_io ? 16 * r.N : 0);
+  h->last_run.d2h_bytes = 0;
+  h->last_run.kernel_launches = 0;
   for (int32_t ev = 0; ev < r.E; ++ev) {
     const int64_t s0 = r.off[ev], n = r.off[ev + 1] - s0;
     if (n == 0) continue;
@@ -469,7 +475,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
       b.seed = r.out->isSeed + s0;
       b.ci = r.out->clusterIndex + s0;
     }
-    e = launch_clue2d(b, h->p2d, h->tuning, s);
+    e = launch_clue2d(b, h->p2d, h->tuning, s, nullptr, &h->last_run.kernel_launches);
     if (e != cudaSuccess) return cuda_error(e, "launching CLUE kernels");
     if (host_io) {
       const clue_outputs* o = r.out;
@@ -484,7 +490,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) return cuda_error(e, "per-event synchronise");
       any_error |= static_cast<int32_t*>(h->flags_host.p)[kFlagError];
-      h->last_d2h += 20 * n + 4 * kFlagCount;
+      h->last_run.d2h_bytes += 20 * n + 4 * kFlagCount;
     }
   }
   if (host_io) {
@@ -495,7 +501,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   // never clears it) and is read back at clue_synchronize.
   e = cudaMemcpyAsync(h->flags_host.p, h->arena.ptr(S_FLAGS), 4 * kFlagCount, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_error(e, "D2H status");
-  h->last_d2h = 4 * kFlagCount;
+  h->last_run.d2h_bytes = 4 * kFlagCount;
   e = cudaEventRecord(h->done_event, s);
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
@@ -569,6 +575,7 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaEventRecord(d2h[k], h->stream)) != cudaSuccess)
       return cuda_error(e, "cudaEventRecord");
   int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
+  int64_t kernels = 0;
   for (int i = 0; i < S; ++i) {
     const int k = i % kPipeSlots;
     const int32_t e0 = cut[i], Es = cut[i + 1] - e0;
@@ -603,7 +610,8 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaStreamWaitEvent(cs, d2h[k], 0)) != cudaSuccess ||
         (e = cudaMemsetAsync(b.flags + kFlagError, 0, 4, cs)) != cudaSuccess)
       return cuda_error(e, "sub-batch set-up");
-    if ((e = launch_clue2d(b, h->p2d, h->tuning, cs)) != cudaSuccess) return cuda_error(e, "launching CLUE kernels");
+    if ((e = launch_clue2d(b, h->p2d, h->tuning, cs, nullptr, &kernels)) != cudaSuccess)
+      return cuda_error(e, "launching CLUE kernels");
     if ((e = cudaEventRecord(comp[k], cs)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
     const clue_outputs* o = r.out;
     if ((e = cudaStreamWaitEvent(co, comp[k], 0)) != cudaSuccess ||
@@ -617,8 +625,9 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaEventRecord(d2h[k], co)) != cudaSuccess)
       return cuda_error(e, "D2H sub-batch");
   }
-  h->last_h2d = 16 * r.N + 12 * (int64_t)(r.E + S);
-  h->last_d2h = 20 * r.N + 4 * kFlagCount * (int64_t)S;
+  h->last_run.h2d_bytes = 16 * r.N + 12 * (int64_t)(r.E + S);
+  h->last_run.d2h_bytes = 20 * r.N + 4 * kFlagCount * (int64_t)S;
+  h->last_run.kernel_launches = kernels;
   // the handle's stream orders after the last copy-out, so later work and
   // clue_synchronize see a finished batch
   for (int k = 0; k < kPipeSlots; ++k)
@@ -789,11 +798,9 @@ int clue_run_batch(clue_handle* hh, int32_t n_events, const int64_t* event_offse
   });
 }
 
-int clue_last_transfer(clue_handle* hh, int64_t* h2d_bytes, int64_t* d2h_bytes) {
-  if (!hh || !h2d_bytes || !d2h_bytes) return set_error(CLUE_EINVAL, "NULL argument");
-  const Handle* h = reinterpret_cast<const Handle*>(hh);
-  *h2d_bytes = h->last_h2d;
-  *d2h_bytes = h->last_d2h;
+int clue_last_run_stats(clue_handle* hh, clue_run_stats* stats) {
+  if (!hh || !stats) return set_error(CLUE_EINVAL, "NULL argument");
+  *stats = reinterpret_cast<const Handle*>(hh)->last_run;
   return CLUE_OK;
 }
 

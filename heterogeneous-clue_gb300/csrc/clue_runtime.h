@@ -114,7 +114,8 @@ struct Handle {
   cudaStream_t copy_in = nullptr;         // pipelined host-memory path: H2D stream
   cudaStream_t copy_out = nullptr;        // and D2H stream
   cudaEvent_t pipe_events[3 * kPipeSlots] = {};  // per slot: H2D done, kernels done, D2H done
-  int64_t last_h2d = 0, last_d2h = 0;     // host<->device bytes of the last 2D run
+  clue_run_stats last_run{};              // copies and kernels of the last 2D run
+  int64_t graph_kernels = 0;              // kernels in graph_exec
   PinnedBuf stage;
   PinnedBuf flags_host;
   PinnedBuf nt_host;

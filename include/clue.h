@@ -104,10 +104,16 @@ int clue_run_batch(clue_handle* h, int32_t n_events, const int64_t* event_offset
  * error recorded on the device (e.g. a layer outside [0, 100)). */
 int clue_synchronize(clue_handle* h);
 
-/* Host<->device bytes the last CLUE 2D run on this handle copied (points,
- * outputs, offset and chunk tables, status words; device-memory runs copy
- * only the tables and the status). */
-int clue_last_transfer(clue_handle* h, int64_t* h2d_bytes, int64_t* d2h_bytes);
+/* What the last CLUE 2D run (clue_run_event / clue_run_batch) on a handle
+ * queued: host<->device bytes (points, outputs, offset and chunk tables,
+ * status words; device-memory runs copy only the tables and the status) and
+ * kernel launches (a graph replay counts the kernels in the graph). */
+typedef struct clue_run_stats {
+  int64_t h2d_bytes;
+  int64_t d2h_bytes;
+  int64_t kernel_launches;
+} clue_run_stats;
+int clue_last_run_stats(clue_handle* h, clue_run_stats* stats);
 
 /* Device bytes a batch of n_points points in n_events events needs. */
 size_t clue_required_bytes(int32_t n_events, int64_t n_points, int flags);

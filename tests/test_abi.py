@@ -42,7 +42,7 @@ def test_null_arguments_are_einval(cuda_lib):
     assert "NULL" in C.last_error()
     assert cuda_lib.clue_destroy(None) == C.CLUE_OK
     assert cuda_lib.clue_set_stream(None, None) == C.CLUE_EINVAL
-    assert cuda_lib.clue_last_transfer(None, None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_last_run_stats(None, None) == C.CLUE_EINVAL
     assert cuda_lib.clue_bridge_count(None, 0, None, None, None) == C.CLUE_EINVAL
     assert cuda_lib.clue_bridge_build(None, None, 0, None, None, None, None, None, None, None, None, None) == \
         C.CLUE_EINVAL

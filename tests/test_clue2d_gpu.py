@@ -266,11 +266,13 @@ def test_host_memory_pipelined_large_batch(algo):
     n = int(b["offsets"][-1])
     assert n >= 32 << 20  # four or more sub-batches
     got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
-    h2d, d2h = algo.last_transfer()
-    assert 16 * n < h2d < 16 * n + 64 * b["offsets"].size
-    assert 20 * n < d2h < 20 * n + 4096  # outputs plus one status block per sub-batch
+    st = algo.last_run_stats()
+    assert 16 * n < st["h2d_bytes"] < 16 * n + 64 * b["offsets"].size
+    assert 20 * n < st["d2h_bytes"] < 20 * n + 4096  # outputs plus one status block per sub-batch
+    assert st["kernel_launches"] >= 8 * 4  # four or more sub-batches of 8 kernels or more
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
-    assert algo.last_transfer() == (16 * n + 12 * b["offsets"].size, 20 * n + 32)
+    st = algo.last_run_stats()
+    assert (st["h2d_bytes"], st["d2h_bytes"]) == (16 * n + 12 * b["offsets"].size, 20 * n + 32)
     assert_bitexact(got, ref)
     for e in (0, 359, 759):
         s, t = b["offsets"][e], b["offsets"][e + 1]
@@ -284,3 +286,24 @@ def test_host_memory_pipelined_large_batch(algo):
     again = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
     assert_bitexact(again, ref)
 
+
+def test_layer_order_rule_and_run_stats(cuda_lib):
+    """Batches with a few layers per CTA take their layers largest first (one
+    more kernel); a single event keeps the event order.  The order only
+    changes which CTA runs which layer: results are identical to the
+    one-event-per-launch form, and the run statistics count what was queued."""
+    algo = C.Clusterizer(*PRM)  # default tuning: several CTAs per SM, so 200 events are a few layers per CTA
+    b = S.uneven_batch(200, seed=41, lo=5000, hi=60000)
+    n = int(b["offsets"][-1])
+    got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
+    ordered = algo.last_run_stats()
+    assert ordered["h2d_bytes"] == 16 * n + 12 * b["offsets"].size
+    ev = S.event_of(b, 7)
+    algo.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
+    single = algo.last_run_stats()
+    assert single["kernel_launches"] in (8, 9)  # with or without the large-layer pass
+    assert ordered["kernel_launches"] == single["kernel_launches"] + 1
+    ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.PLAIN)
+    assert algo.last_run_stats()["kernel_launches"] == 200 * single["kernel_launches"]
+    algo.close()
+    assert_bitexact(got, ref)
