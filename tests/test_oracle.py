@@ -94,6 +94,32 @@ def test_oracle_known_answers():
     assert o["isSeed"].tolist() == [1, 1] and o["clusterIndex"].tolist() == [0, 1]
 
 
+_KA = None
+
+
+def _known_answer_cases():
+    global _KA
+    if _KA is None:
+        import test_known_answers_gpu as ka  # the micro cases, written against a `run` callable
+        _KA = {n: getattr(ka, n) for n in dir(ka) if n.startswith("test_")}
+    return _KA
+
+
+@needs_ref
+@pytest.mark.parametrize("name", sorted(_known_answer_cases()))
+def test_known_answer_micro_cases_on_the_reference(name):
+    """The hand-derived micro cases (exact <= / > boundaries, ties, first-wins
+    order) run through the reference's own makeClusters; the oracle must
+    agree with it bit for bit on each."""
+    def run(x, y, layer, w, dc, rhoc, odf):
+        x, y = np.asarray(x, np.float32), np.asarray(y, np.float32)
+        layer, w = np.asarray(layer, np.int32), np.asarray(w, np.float32)
+        ref = oracle.ref_clue2d(x, y, layer, w, dc, rhoc, odf)
+        assert_bitexact(oracle.clue2d(x, y, layer, w, dc, rhoc, odf), ref, label=name)
+        return ref
+    _known_answer_cases()[name](run)
+
+
 def test_oracle_rejects_bad_layer():
     with pytest.raises(ValueError):
         oracle.clue2d([0.0], [0.0], [100], [1.0], 1.3, 2.0, 2.0)
