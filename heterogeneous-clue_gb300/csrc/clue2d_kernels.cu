@@ -349,6 +349,11 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   __syncthreads();
   {
     const unsigned lt = (1u << lane) - 1u;
+    // gid = gid_base + p ascends with p (layer-ordered input); otherwise the
+    // gids come from the layer-grouping gather in arbitrary order
+    const bool mono = in.gid == nullptr;
+    int32_t* lead_p = slot_p + 2 * m;  // by point: size of the group it leads, else 0
+    int32_t* lead_q = slot_p + 3 * m;  // the same by provisional slot
     for (int base = 0; base < m; base += NT) {
       const int p = base + tid;
       const int key = p < m ? tile_bin(in.x[p]) * kGridCols + tile_bin(in.y[p]) : -1;
@@ -360,6 +365,7 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
       if (key >= 0) {
         kkey[p] = (QT)key;
         kprov[p] = old + __popc(grp & lt);
+        if (mono) lead_p[p] = lane == leader ? __popc(grp) : 0;
       }
     }
     __syncthreads();
@@ -368,17 +374,32 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
       const int q = (int)S.tbl[kkey[p]] + kprov[p];
       slot_g[q] = in.gid ? in.gid[p] : in.gid_base + p;
       slot_p[q] = p;
+      if (mono) lead_q[q] = lead_p[p];
     }
     __syncthreads();
     // Atomics gave an arbitrary order inside a tile; the reference appends in
-    // index order, so place each point at its gid rank within the tile.
+    // index order, so place each point at its gid rank within the tile.  With
+    // layer-ordered input a tile's slots are groups (one atomic each) of lanes
+    // of one warp pass over 32 consecutive points: gids ascend inside a group
+    // and different groups cover disjoint gid ranges, so the rank is the sizes
+    // of the groups that start below g plus g's place in its own group -- a
+    // walk over the tile's groups instead of its points.
     for (int q = tid; q < m; q += NT) {
       const int p = slot_p[q];
       const int key = (int)kkey[p];
       const int s = (int)S.tbl[key], e = (int)S.tbl[key + 1];
       const int g = slot_g[q];
       int rank = 0;
-      for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
+      if (mono) {
+        for (int t = s; t < e;) {
+          const int c = max(lead_q[t], 1);
+          if (q >= t && q < t + c) rank += q - t;
+          else if (slot_g[t] < g) rank += c;
+          t += c;
+        }
+      } else {
+        for (int t = s; t < e; ++t) rank += (slot_g[t] < g);
+      }
       kkey[p] = (QT)(s + rank);
     }
     __syncthreads();

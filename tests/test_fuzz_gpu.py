@@ -42,16 +42,21 @@ def _cloud(rng, kind, n):
     return dict(x=x, y=y, layer=layer, weight=w)
 
 
-CASES = [(kind, seed) for kind in ("lattice", "duplicates", "wide", "blobs") for seed in range(3)]
+CASES = [(kind, seed, order) for kind in ("lattice", "duplicates", "wide", "blobs") for seed in range(3)
+         for order in ("random", "layer-sorted")]
 
 
-@pytest.mark.parametrize("kind,seed", CASES, ids=[f"{k}-{s}" for k, s in CASES])
-def test_random_clouds_and_parameters(cuda_lib, kind, seed):
+@pytest.mark.parametrize("kind,seed,order", CASES, ids=[f"{k}-{s}-{o}" for k, s, o in CASES])
+def test_random_clouds_and_parameters(cuda_lib, kind, seed, order):
+    """Random layers take the layer-grouping gather; layer-sorted clouds are
+    read in place (their in-tile ranks come from the warp groups)."""
     rng = np.random.default_rng(1000 * seed + len(kind))
     dc = float(rng.choice([0.5, 1.3, 2.6, 4.0, 7.5]))
     rhoc = float(rng.uniform(0.5, 10.0))
     odf = float(rng.choice([0.5, 1.0, 2.0, 3.0]))
     evs = [_cloud(rng, kind, int(rng.integers(500, 20000))) for _ in range(3)]
+    if order == "layer-sorted":
+        evs = [{k: v[np.argsort(e["layer"], kind="stable")] for k, v in e.items()} for e in evs]
     sizes = [e["x"].size for e in evs]
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     cat = {k: np.concatenate([e[k] for e in evs]) for k in evs[0]}
