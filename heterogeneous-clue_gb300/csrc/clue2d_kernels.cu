@@ -331,9 +331,11 @@ __device__ __forceinline__ int next_chunk(int* s_next) {
   return __shfl_sync(0xffffffffu, base, 0);
 }
 
+// One (event, layer) item through every stage.  next_item: in thread 0, the
+// item this CTA takes next (-1 when none), whose inputs are prefetched.
 template <int NT, class TT, class QT>
 __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, const int m, const LayerIO& in,
-                              const Batch2D& b, int* s_ws, int* s_bins, int* s_next) {
+                              const Batch2D& b, int* s_ws, int* s_bins, int* s_next, int next_item) {
   const int tid = threadIdx.x, lane = tid & 31;
   QT* kkey = S.qord;                                     // sort key, later final slot
   int32_t* kprov = S.nh;                                 // provisional slot in tile
@@ -412,6 +414,25 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
     S.nh[f] = __float_as_int(wv);
   }
   __syncthreads();
+
+  // the next layer's inputs (the ticket taken while this layer started) into
+  // L2 while this one is searched: its histogram and records then read L2
+  if (tid < 32) {
+    const int nx = __shfl_sync(0xffffffffu, next_item, 0);
+    if (nx >= 0) {
+      const int nm = b.lcnt[nx];
+      const int ns = b.lstart[nx];
+      const bool gr = b.flags[kFlagGrouped] != 0;
+      const float* ax = (gr ? b.x : b.gx) + ns;
+      const float* ay = (gr ? b.y : b.gy) + ns;
+      const float* aw = (gr ? b.w : b.gw) + ns;
+      for (int o = lane * 32; o < nm; o += 32 * 32) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(ax + o));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(ay + o));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(aw + o));
+      }
+    }
+  }
 
   // One query order for both searches, by the nearest-higher box (the
   // larger box and the more expensive search).
@@ -783,7 +804,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
       io.gid_base = 0;
     }
     if (m <= cap) {
-      process_layer<NT>(P, sm, m, io, b, s_ws, s_bins, &s_next);
+      process_layer<NT>(P, sm, m, io, b, s_ws, s_bins, &s_next, next);
     } else {
       // spill: the same stages on HBM scratch at this layer's grouped position
       LayerStore<int32_t, int32_t> g;
@@ -792,7 +813,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
       g.qord = reinterpret_cast<int32_t*>(b.sp[5]) + start;
       g.tbl = b.sp_tbl + (size_t)blockIdx.x * kTableStride;
       if (threadIdx.x == 0) atomicAdd(&b.flags[kFlagSpilled], 1);
-      process_layer<NT>(P, g, m, io, b, s_ws, s_bins, &s_next);
+      process_layer<NT>(P, g, m, io, b, s_ws, s_bins, &s_next, next);
     }
   }
 }
