@@ -22,7 +22,7 @@ ROOT = os.path.dirname(PKG)
 LIB_PATH = os.path.join(PKG, "lib", "libclue_gb300.so")
 HEADER = os.path.join(ROOT, "include", "clue.h")
 
-STAGES = ("count", "layer_scan", "scatter", "layers", "seed_count", "seed_chunk_scan", "seed_rank", "label")
+STAGES = ("count", "layer_scan", "scatter", "layers", "seed_chunk_scan", "seed_rank", "label")
 
 CLUE_OK, CLUE_EINVAL, CLUE_ENOMEM, CLUE_ECUDA, CLUE_ETIMEOUT, CLUE_EBUSY = range(6)
 HOST_MEMORY, DEVICE_MEMORY, PLAIN, NO_GRAPH, NO_PIPELINE = 0, 1, 2, 4, 8

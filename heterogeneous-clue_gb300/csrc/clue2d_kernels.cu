@@ -9,9 +9,10 @@
 //   k_layers       persistent CTAs over the (event, layer) queue.  Per layer,
 //                  on-chip: counting sort into the reference's 5 cm tiles
 //                  (column-major, index order inside a tile), density,
-//                  nearest-higher, seed/outlier flags and pointer jumping
+//                  nearest-higher, seed/outlier flags (and seeds counted per
+//                  event-aligned chunk of 4096 points) and pointer jumping
 //                  to each point's root
-//   k_seed_count / k_seed_chunk_scan / k_seed_rank
+//   k_seed_chunk_scan / k_seed_rank
 //                  event-wide seed numbering in index order
 //   k_label        clusterIndex = cluster of the root seed, -1 when the
 //                  chain ends at an outlier
@@ -205,6 +206,7 @@ struct LayerIO {
   const int32_t* gid;  // nullptr: gid = gid_base + p
   int32_t gid_base;
   int64_t ev_start;
+  int32_t chunk0;  // first seed-count chunk of the event
 };
 
 __device__ __forceinline__ float2 rec_xy(const uint4& r) { return make_float2(__uint_as_float(r.x), __uint_as_float(r.y)); }
@@ -529,6 +531,8 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
       b.delta[o] = best_s;
       b.nh[o] = best >= 0 ? (int)S.rec[best].z : -1;
       b.seed[o] = seed ? 1 : 0;
+      // seeds per event-aligned chunk of 4096 points, for the seed ranks
+      if (seed) atomicAdd(&b.chunk_seeds[in.chunk0 + (int)(rq.z / kChunk)], 1);
       par[q] = (!seed && !outlier && best >= 0) ? best : (seed ? -2 : -3);
     }
   }
@@ -790,6 +794,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
     const int start = b.lstart[item];
     LayerIO io;
     io.ev_start = es;
+    io.chunk0 = b.chunk_start[e];
     if (grouped) {
       io.x = b.x + start;
       io.y = b.y + start;
@@ -817,24 +822,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_layers(Batch2D b, Params2D P,
     }
   }
 }
-// Seeds per event-aligned chunk.
-__global__ void __launch_bounds__(kChunkThreads) k_seed_count(Batch2D b) {
-  const int c = blockIdx.x;
-  __shared__ int s_e;
-  __shared__ int s_ws[33];
-  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
-  __syncthreads();
-  const int e = s_e;
-  const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
-  const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
-  const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
-  int cnt = 0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += kChunkThreads) cnt += b.seed[i];
-  int total;
-  block_inclusive_scan<kChunkThreads>(cnt, s_ws, &total);
-  if (threadIdx.x == 0) b.chunk_seeds[c] = total;
-}
-
 // One warp per event: exclusive scan of its chunks' seed counts.
 __global__ void k_seed_chunk_scan(Batch2D b) {
   const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1061,6 +1048,9 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   err = cudaMemsetAsync(b.flags + kFlagGrouped, 1, 1, s);
   if (err != cudaSuccess) return err;
   const int nc = b.n_chunks;
+  // seeds per chunk are counted by k_layers as it flags them
+  err = cudaMemsetAsync(b.chunk_seeds, 0, sizeof(int32_t) * (size_t)nc, s);
+  if (err != cudaSuccess) return err;
   const int warps_grid = (b.n_events * 32 + 255) / 256;
   mark(0);
   k_count<<<nc, kChunkThreads, 0, s>>>(b);
@@ -1086,15 +1076,13 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   }
   if (err != cudaSuccess) return err;
   mark(4);
-  k_seed_count<<<nc, kChunkThreads, 0, s>>>(b);
-  mark(5);
   k_seed_chunk_scan<<<warps_grid, 256, 0, s>>>(b);
-  mark(6);
+  mark(5);
   k_seed_rank<<<nc, kChunkThreads, 0, s>>>(b);
-  mark(7);
+  mark(6);
   k_label<<<nc, kChunkThreads, 0, s>>>(b);
-  mark(8);
-  if (kernels) *kernels += 8 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
+  mark(7);
+  if (kernels) *kernels += 7 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
   return cudaGetLastError();
 }
 

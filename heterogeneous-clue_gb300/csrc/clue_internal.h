@@ -103,7 +103,7 @@ size_t layer_smem_bytes(const Tuning2D& t);
 // device, outside any stream capture).
 cudaError_t prepare_clue2d_kernels(int device);
 
-constexpr int kStages2D = 8;
+constexpr int kStages2D = 7;
 // Queues the whole 2D pipeline of one batch on `s`.  With `stage_events`
 // (kStages2D + 1 events) an event is recorded before each stage and after the
 // last; `kernels`, when given, is increased by the number of kernels queued.

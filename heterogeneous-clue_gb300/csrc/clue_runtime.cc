@@ -21,6 +21,8 @@
 #include "clue_internal.h"
 #include "clue_runtime.h"
 
+static_assert(clue::kStages2D == CLUE_N_STAGES, "stage list of the ABI and of the pipeline differ");
+
 namespace clue {
 
 thread_local std::string g_last_error;

@@ -119,8 +119,8 @@ int clue_last_run_stats(clue_handle* h, clue_run_stats* stats);
 size_t clue_required_bytes(int32_t n_events, int64_t n_points, int flags);
 
 /* Stages of the batched pipeline, in launch order. */
-#define CLUE_N_STAGES 8 /* count, layer_scan (with the largest-first order when taken), scatter, layers,
-                           seed_count, seed_chunk_scan, seed_rank, label */
+#define CLUE_N_STAGES 7 /* count, layer_scan (with the largest-first order when taken), scatter,
+                           layers (which also counts seeds per chunk), seed_chunk_scan, seed_rank, label */
 
 /* Runs one batch like clue_run_batch (device memory, direct launches) and
  * writes each stage's duration in milliseconds to stage_ms[CLUE_N_STAGES],

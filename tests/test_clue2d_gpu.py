@@ -269,7 +269,7 @@ def test_host_memory_pipelined_large_batch(algo):
     st = algo.last_run_stats()
     assert 16 * n < st["h2d_bytes"] < 16 * n + 64 * b["offsets"].size
     assert 20 * n < st["d2h_bytes"] < 20 * n + 4096  # outputs plus one status block per sub-batch
-    assert st["kernel_launches"] >= 8 * 4  # four or more sub-batches of 8 kernels or more
+    assert st["kernel_launches"] >= 7 * 4  # four or more sub-batches of 7 kernels or more
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
     st = algo.last_run_stats()
     assert (st["h2d_bytes"], st["d2h_bytes"]) == (16 * n + 12 * b["offsets"].size, 20 * n + 32)
@@ -301,7 +301,7 @@ def test_layer_order_rule_and_run_stats(cuda_lib):
     ev = S.event_of(b, 7)
     algo.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
     single = algo.last_run_stats()
-    assert single["kernel_launches"] in (8, 9)  # with or without the large-layer pass
+    assert single["kernel_launches"] in (7, 8)  # with or without the large-layer pass
     assert ordered["kernel_launches"] == single["kernel_launches"] + 1
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.PLAIN)
     assert algo.last_run_stats()["kernel_launches"] == 200 * single["kernel_launches"]
