@@ -65,6 +65,11 @@ __device__ __forceinline__ int chunk_event(const int32_t* chunk_start, int n_eve
   return lo;
 }
 
+// Event of a chunk: from the host-built table when the batch has one.
+__device__ __forceinline__ int event_of_chunk(const Batch2D& b, int c) {
+  return b.chunk_ev ? b.chunk_ev[c] : chunk_event(b.chunk_start, b.n_events, c);
+}
+
 template <int NT>
 __device__ __forceinline__ int block_inclusive_scan(int v, int* s_ws, int* total) {
   constexpr int NW = NT / 32;
@@ -586,7 +591,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
   // the size histogram of k_layer_scan starts from zero (it runs after this kernel)
   if (c == 0 && b.use_order)
     for (int i = threadIdx.x; i < 2 * kSizeBuckets; i += kChunkThreads) b.size_hist[i] = 0;
-  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  if (threadIdx.x == 0) s_e = event_of_chunk(b, c);
   __syncthreads();
   const int e = s_e;
   const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
@@ -713,7 +718,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
   if (b.flags[kFlagGrouped]) return;  // input already grouped by layer
   const int c = blockIdx.x;
   __shared__ int s_e;
-  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  if (threadIdx.x == 0) s_e = event_of_chunk(b, c);
   __syncthreads();
   const int e = s_e;
   const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
@@ -849,7 +854,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_seed_rank(Batch2D b) {
   const int c = blockIdx.x;
   __shared__ int s_e;
   __shared__ int s_ws[33];
-  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  if (threadIdx.x == 0) s_e = event_of_chunk(b, c);
   __syncthreads();
   const int e = s_e;
   const int64_t es = b.offsets[e], ee = b.offsets[e + 1];
@@ -876,7 +881,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_seed_rank(Batch2D b) {
 __global__ void __launch_bounds__(kChunkThreads) k_label(Batch2D b) {
   const int c = blockIdx.x;
   __shared__ int s_e;
-  if (threadIdx.x == 0) s_e = chunk_event(b.chunk_start, b.n_events, c);
+  if (threadIdx.x == 0) s_e = event_of_chunk(b, c);
   __syncthreads();
   const int e = s_e;
   const int64_t es = b.offsets[e], ee = b.offsets[e + 1];

@@ -66,6 +66,7 @@ struct Batch2D {
   int32_t n_chunks = 0;
   const int64_t* offsets = nullptr;      // [E+1]
   const int32_t* chunk_start = nullptr;  // [E+1] first chunk of each event
+  const int32_t* chunk_ev = nullptr;     // [n_chunks] event of each chunk (nullptr: searched in chunk_start)
   const float* x = nullptr;
   const float* y = nullptr;
   const int32_t* layer = nullptr;

@@ -118,7 +118,7 @@ namespace {
 enum Slot2D : int {
   S_OFF, S_CS, S_LCNT, S_LSTART, S_CURSOR, S_GX, S_GY, S_GW, S_GID,
   S_SP0, S_SP1, S_SP2, S_SP3, S_SP4, S_SP5, S_SP6, S_SP7,
-  S_SPTBL, S_CSEED, S_CBASE, S_FLAGS, S_ORDER,
+  S_SPTBL, S_CSEED, S_CBASE, S_FLAGS, S_ORDER, S_CEV,
   S_IN_X, S_IN_Y, S_IN_L, S_IN_W, S_OUT_RHO, S_OUT_DELTA, S_OUT_NH, S_OUT_SEED, S_OUT_CI,
   S_COUNT
 };
@@ -140,7 +140,7 @@ std::vector<size_t> sizes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bo
   s[S_SP1] = s[S_SP2] = s[S_SP3] = s[S_SP6] = s[S_SP7] = 0;
   s[S_SP4] = s[S_SP5] = 4 * (size_t)N;
   s[S_SPTBL] = 4 * (size_t)kTableStride * grid;
-  s[S_CSEED] = s[S_CBASE] = 4 * (size_t)std::max<int64_t>(nchunks, 1);
+  s[S_CSEED] = s[S_CBASE] = s[S_CEV] = 4 * (size_t)std::max<int64_t>(nchunks, 1);
   s[S_FLAGS] = 4 * kFlagCount;
   s[S_ORDER] = 4 * ((size_t)E * kLayers + 2 * kSizeBuckets);
   if (host_io) {
@@ -172,7 +172,7 @@ int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io) {
   const int64_t nchunks = N / kChunk + E;
   const int grid = layer_grid_max(h->tuning, std::max(1, E * kLayers));
   int rc = h->arena.reserve(sizes_2d(E, N, nchunks, grid, host_io), h->budget);
-  if (!rc) rc = h->stage.reserve(24 * (size_t)(E + 1));
+  if (!rc) rc = h->stage.reserve(24 * (size_t)(E + 1) + 4 * (size_t)nchunks);
   if (!rc) rc = h->flags_host.reserve(4 * kFlagCount);
   return rc;
 }
@@ -243,6 +243,9 @@ int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t*
   e = cudaMemcpyAsync((void*)b.chunk_start, static_cast<char*>(h->stage.p) + 8 * (size_t)(r.E + 1),
                       4 * (size_t)(r.E + 1), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "H2D chunk table");
+  e = cudaMemcpyAsync((void*)b.chunk_ev, static_cast<char*>(h->stage.p) + 12 * (size_t)(r.E + 1),
+                      4 * (size_t)b.n_chunks, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_error(e, "H2D chunk events");
   if (host_io) {
     if ((e = cudaMemcpyAsync((void*)b.x, r.x, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.y, r.y, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
@@ -307,6 +310,7 @@ void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, 
   b.sp_tbl = static_cast<int32_t*>(P(S_SPTBL));
   b.chunk_seeds = static_cast<int32_t*>(P(S_CSEED));
   b.chunk_base = static_cast<int32_t*>(P(S_CBASE));
+  b.chunk_ev = static_cast<const int32_t*>(P(S_CEV));
   b.flags = static_cast<int32_t*>(P(S_FLAGS));
   b.order = static_cast<int32_t*>(P(S_ORDER));
   b.size_hist = b.order + (size_t)r.E * kLayers;
@@ -321,13 +325,17 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   rc = h->arena.reserve(sizes_2d(r.E, r.N, nchunks, grid, host_io), h->budget);
   if (rc) return rc;
   // offsets + chunk table through pinned staging (graph nodes copy from it)
-  rc = h->stage.reserve(12 * (size_t)(r.E + 1));
+  rc = h->stage.reserve(12 * (size_t)(r.E + 1) + 4 * (size_t)nchunks);
   if (rc) return rc;
   int64_t* so = static_cast<int64_t*>(h->stage.p);
   int32_t* sc = reinterpret_cast<int32_t*>(static_cast<char*>(h->stage.p) + 8 * (size_t)(r.E + 1));
+  int32_t* sce = sc + (r.E + 1);  // event of each chunk
   memcpy(so, r.off, 8 * (size_t)(r.E + 1));
   sc[0] = 0;
-  for (int32_t e = 0; e < r.E; ++e) sc[e + 1] = sc[e] + (int32_t)((r.off[e + 1] - r.off[e] + kChunk - 1) / kChunk);
+  for (int32_t e = 0; e < r.E; ++e) {
+    sc[e + 1] = sc[e] + (int32_t)((r.off[e + 1] - r.off[e] + kChunk - 1) / kChunk);
+    for (int32_t c = sc[e]; c < sc[e + 1]; ++c) sce[c] = e;
+  }
   rc = h->flags_host.reserve(4 * kFlagCount);
   if (rc) return rc;
 
@@ -389,7 +397,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
   if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   h->pending = true;
   h->error_layers = kLayers;
-  h->last_run.h2d_bytes = 12 * (int64_t)(r.E + 1) + (host_io ? 16 * r.N : 0);
+  h->last_run.h2d_bytes = 12 * (int64_t)(r.E + 1) + 4 * nchunks + (host_io ? 16 * r.N : 0);
   h->last_run.d2h_bytes = 4 * kFlagCount + (host_io ? 20 * r.N : 0);
   h->last_run.kernel_launches = kernels;
   if (host_io && !(r.flags & kAsyncHostIO)) {
@@ -448,6 +456,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
     one.N = n;
     Batch2D b;
     fill_batch_views(h, one, sc[2 * ev + 1], false, b);
+    b.chunk_ev = nullptr;  // one event: every chunk is event 0
     b.offsets = static_cast<const int64_t*>(h->arena.ptr(S_OFF)) + 2 * ev;
     b.chunk_start = static_cast<const int32_t*>(h->arena.ptr(S_CS)) + 2 * ev;
     const size_t n4 = 4 * (size_t)n;
@@ -552,7 +561,10 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
   }
   // pinned staging: per sub-batch its rebased offsets and chunk table
   std::vector<size_t> st_off(S + 1, 0);
-  for (int i = 0; i < S; ++i) st_off[i + 1] = st_off[i] + 16 * (size_t)(cut[i + 1] - cut[i] + 1);
+  for (int i = 0; i < S; ++i) {
+    const int64_t nci = n_chunks_of(cut[i + 1] - cut[i], r.off + cut[i]);
+    st_off[i + 1] = st_off[i] + (((12 * (size_t)(cut[i + 1] - cut[i] + 1) + 4 * (size_t)nci) + 7) & ~size_t(7));
+  }
   if ((rc = h->stage.reserve(st_off[S]))) return rc;
   if ((rc = h->flags_host.reserve(4 * kFlagCount * (size_t)S))) return rc;
   cudaError_t e;
@@ -586,8 +598,12 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
     int64_t* so = reinterpret_cast<int64_t*>(static_cast<char*>(h->stage.p) + st_off[i]);
     int32_t* sc = reinterpret_cast<int32_t*>(so + (Es + 1));
     sc[0] = 0;
+    int32_t* sce = sc + (Es + 1);  // event of each chunk
     for (int32_t j = 0; j <= Es; ++j) so[j] = r.off[e0 + j] - p0;
-    for (int32_t j = 0; j < Es; ++j) sc[j + 1] = sc[j] + (int32_t)((so[j + 1] - so[j] + kChunk - 1) / kChunk);
+    for (int32_t j = 0; j < Es; ++j) {
+      sc[j + 1] = sc[j] + (int32_t)((so[j + 1] - so[j] + kChunk - 1) / kChunk);
+      for (int32_t c = sc[j]; c < sc[j + 1]; ++c) sce[c] = j;
+    }
     Run2D sub = r;
     sub.E = Es;
     sub.N = Ns;
@@ -601,6 +617,8 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
     if ((e = cudaStreamWaitEvent(ci, comp[k], 0)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.offsets, so, 8 * (size_t)(Es + 1), cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.chunk_start, sc, 4 * (size_t)(Es + 1), cudaMemcpyHostToDevice, ci)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.chunk_ev, sce, 4 * (size_t)sc[Es], cudaMemcpyHostToDevice, ci)) !=
             cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.x, r.x + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.y, r.y + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
@@ -627,7 +645,7 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaEventRecord(d2h[k], co)) != cudaSuccess)
       return cuda_error(e, "D2H sub-batch");
   }
-  h->last_run.h2d_bytes = 16 * r.N + 12 * (int64_t)(r.E + S);
+  h->last_run.h2d_bytes = 16 * r.N + 12 * (int64_t)(r.E + S) + 4 * n_chunks_of(r.E, r.off);
   h->last_run.d2h_bytes = 20 * r.N + 4 * kFlagCount * (int64_t)S;
   h->last_run.kernel_launches = kernels;
   // the handle's stream orders after the last copy-out, so later work and

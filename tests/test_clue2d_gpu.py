@@ -267,12 +267,13 @@ def test_host_memory_pipelined_large_batch(algo):
     assert n >= 32 << 20  # four or more sub-batches
     got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"])
     st = algo.last_run_stats()
-    assert 16 * n < st["h2d_bytes"] < 16 * n + 64 * b["offsets"].size
+    nchunks = int(np.sum((np.diff(b["offsets"]) + 4095) // 4096))  # event-aligned chunks of 4096 points
+    assert 16 * n + 4 * nchunks < st["h2d_bytes"] < 16 * n + 4 * nchunks + 64 * b["offsets"].size
     assert 20 * n < st["d2h_bytes"] < 20 * n + 4096  # outputs plus one status block per sub-batch
     assert st["kernel_launches"] >= 7 * 4  # four or more sub-batches of 7 kernels or more
     ref = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
     st = algo.last_run_stats()
-    assert (st["h2d_bytes"], st["d2h_bytes"]) == (16 * n + 12 * b["offsets"].size, 20 * n + 32)
+    assert (st["h2d_bytes"], st["d2h_bytes"]) == (16 * n + 12 * b["offsets"].size + 4 * nchunks, 20 * n + 32)
     assert_bitexact(got, ref)
     for e in (0, 359, 759):
         s, t = b["offsets"][e], b["offsets"][e + 1]
@@ -297,7 +298,8 @@ def test_layer_order_rule_and_run_stats(cuda_lib):
     n = int(b["offsets"][-1])
     got = algo.run_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], flags=C.NO_PIPELINE)
     ordered = algo.last_run_stats()
-    assert ordered["h2d_bytes"] == 16 * n + 12 * b["offsets"].size
+    nchunks = int(np.sum((np.diff(b["offsets"]) + 4095) // 4096))
+    assert ordered["h2d_bytes"] == 16 * n + 12 * b["offsets"].size + 4 * nchunks
     ev = S.event_of(b, 7)
     algo.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
     single = algo.last_run_stats()
