@@ -10,14 +10,16 @@
 // the slot (points and event count), stages them, and launches the batched
 // pipeline asynchronously; batches of different slots overlap on the device
 // (one batch's copies with another's kernels).  Completed batches are found
-// with cudaEventQuery, their outputs are copied to each caller's buffers,
-// and the request latency (submit -> outputs written) is recorded.
+// with cudaEventQuery (every 20 us while batches are in flight), their outputs
+// are copied to each caller's buffers, and the request latency (submit ->
+// outputs written) is recorded.  Host copies run on a resident pool.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdint>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -35,42 +37,111 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 // Host copies of the serving path (request staging and result delivery).
-// Large sets are cut into 1 MB pieces and spread over a few threads.
+// Sets of 512 KB or more are cut into 256 KB pieces shared by the calling
+// thread and resident helper threads (no thread is started per copy).
+// Several callers (submitting clients, the scheduler) may run sets at once:
+// a helper takes at most four pieces of a set before it moves on to the next
+// set, so that no set waits behind a large one.
 struct CopyTask {
   void* dst;
   const void* src;
   size_t bytes;
 };
 
-void run_copies(const std::vector<CopyTask>& tasks) {
-  constexpr size_t kPiece = size_t(1) << 20;
-  size_t total = 0;
-  for (const auto& t : tasks) total += t.bytes;
-  const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
-  const size_t nth = std::min<size_t>({size_t(8), size_t(hw / 2), total / (4 * kPiece)});
-  if (nth <= 1) {
+class CopyPool {
+ public:
+  ~CopyPool() { stop(); }
+
+  void start(int helpers) {
+    for (int k = 0; k < helpers; ++k) {
+      try {
+        threads_.emplace_back([this] { loop(); });
+      } catch (...) {
+        break;  // fewer helpers: callers copy their own pieces
+      }
+    }
+  }
+
+  void stop() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : threads_) t.join();
+    threads_.clear();
+  }
+
+  void run(const std::vector<CopyTask>& tasks) {
+    constexpr size_t kPiece = size_t(256) << 10;
+    size_t total = 0;
+    for (const auto& t : tasks) total += t.bytes;
+    if (threads_.empty() || total < 2 * kPiece) {
+      for (const auto& t : tasks)
+        if (t.bytes) memcpy(t.dst, t.src, t.bytes);
+      return;
+    }
+    Job job;
     for (const auto& t : tasks)
-      if (t.bytes) memcpy(t.dst, t.src, t.bytes);
-    return;
+      for (size_t o = 0; o < t.bytes; o += kPiece)
+        job.pieces.push_back({static_cast<char*>(t.dst) + o, static_cast<const char*>(t.src) + o,
+                              std::min(kPiece, t.bytes - o)});
+    job.left = job.pieces.size();
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      jobs_.push_back(&job);
+    }
+    cv_.notify_all();
+    work(job);
+    // the job lives on this stack: wait until no helper holds it any more
+    std::unique_lock<std::mutex> g(mu_);
+    done_cv_.wait(g, [&] { return job.left.load() == 0 && job.holders == 0; });
+    auto it = std::find(jobs_.begin(), jobs_.end(), &job);
+    if (it != jobs_.end()) jobs_.erase(it);
   }
-  std::vector<CopyTask> pieces;
-  for (const auto& t : tasks)
-    for (size_t o = 0; o < t.bytes; o += kPiece)
-      pieces.push_back({static_cast<char*>(t.dst) + o, static_cast<const char*>(t.src) + o,
-                        std::min(kPiece, t.bytes - o)});
-  std::atomic<size_t> next{0};
-  auto work = [&] {
-    for (size_t i; (i = next.fetch_add(1)) < pieces.size();) memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+
+ private:
+  struct Job {
+    std::vector<CopyTask> pieces;
+    std::atomic<size_t> next{0};
+    std::atomic<size_t> left{0};
+    int holders = 0;  // helpers working on it (guarded by mu_)
   };
-  std::vector<std::thread> th;
-  try {
-    for (size_t k = 1; k < nth; ++k) th.emplace_back(work);
-  } catch (...) {
-    // no more helper threads: the pieces left are copied by the ones running
+
+  static void work(Job& j, size_t max_pieces = SIZE_MAX) {
+    for (size_t i, k = 0; k < max_pieces && (i = j.next.fetch_add(1)) < j.pieces.size(); ++k) {
+      memcpy(j.pieces[i].dst, j.pieces[i].src, j.pieces[i].bytes);
+      j.left.fetch_sub(1);
+    }
   }
-  work();
-  for (auto& t : th) t.join();
-}
+
+  void loop() {
+    std::unique_lock<std::mutex> g(mu_);
+    for (;;) {
+      cv_.wait(g, [&] { return stop_ || !jobs_.empty(); });
+      if (stop_) return;
+      Job* j = jobs_.front();
+      jobs_.pop_front();
+      if (j->next.load() >= j->pieces.size()) {  // nothing left to take: let the owner finish it
+        done_cv_.notify_all();
+        continue;
+      }
+      jobs_.push_back(j);  // round robin over the sets in progress
+      ++j->holders;
+      g.unlock();
+      work(*j, 4);
+      g.lock();
+      --j->holders;
+      done_cv_.notify_all();
+    }
+  }
+
+  std::vector<std::thread> threads_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  std::deque<Job*> jobs_;
+  bool stop_ = false;
+};
 
 struct Request {
   int64_t id = 0;
@@ -130,6 +201,8 @@ class Server {
       if (rc) return rc;
     }
     cap_points_ = slots_[0].cap_points;
+    // helpers on all cores but two (the scheduler and a submitting client), at most 15
+    pool_.start((int)std::min(15u, std::max(3u, std::thread::hardware_concurrency()) - 2));
     worker_ = std::thread([this] { loop(); });
     return CLUE_OK;
   }
@@ -192,7 +265,7 @@ class Server {
       r->t_submit = now;
       rs[e] = r;
     }
-    run_copies(copies);
+    pool_.run(copies);
     {
       std::lock_guard<std::mutex> g(mu_);
       for (int32_t e = 0; e < E; ++e) {
@@ -312,7 +385,7 @@ class Server {
         copies.push_back({r->out.clusterIndex, ob + 4 * (4 * N + o), b});
       }
     }
-    run_copies(copies);
+    pool_.run(copies);
     const auto now = Clock::now();
     g.lock();
     for (size_t d = 0; d < done.size(); ++d) {
@@ -368,7 +441,7 @@ class Server {
         copies.push_back({ib + 4 * (2 * pts + o), r->layer.data(), b});
         copies.push_back({ib + 4 * (3 * pts + o), r->w.data(), b});
       }
-      run_copies(copies);
+      pool_.run(copies);
       for (Request* r : s.reqs) {  // inputs are staged: free them now
         std::vector<float>().swap(r->x);
         std::vector<float>().swap(r->y);
@@ -422,7 +495,7 @@ class Server {
       }
       if (busy) {
         // batches in flight: look again shortly (new arrivals wake us earlier)
-        cv_.wait_for(g, std::chrono::microseconds(50));
+        cv_.wait_for(g, std::chrono::microseconds(20));
       } else {
         cv_.wait_for(g, std::chrono::milliseconds(5));
       }
@@ -447,6 +520,7 @@ class Server {
   int64_t next_id_ = 1;
   bool stop_ = false;
   std::thread worker_;
+  CopyPool pool_;  // its helpers stop when the server is destroyed, after shutdown() joined worker_
   std::vector<double> lat_;
   int64_t batches_ = 0, batched_events_ = 0;
   double max_inflight_seen_ = 0;
