@@ -121,6 +121,7 @@ struct Handle {
   PinnedBuf nt_host;
   cudaGraphExec_t graph_exec = nullptr;
   GraphKey graph_key;
+  GraphKey last_key;  // the previous graph-eligible run (a shape is captured when it repeats)
 
   ~Handle();
   int wait_previous();

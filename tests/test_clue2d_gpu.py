@@ -309,3 +309,27 @@ def test_layer_order_rule_and_run_stats(cuda_lib):
     assert algo.last_run_stats()["kernel_launches"] == 200 * single["kernel_launches"]
     algo.close()
     assert_bitexact(got, ref)
+
+
+def test_graph_only_for_repeated_shapes(cuda_lib):
+    """A new shape runs by direct launches, a shape seen twice in a row is
+    captured, then replayed; another shape re-captures.  Every mode gives the
+    same outputs and reports the same kernel count."""
+    import torch
+    algo = C.Clusterizer(*PRM)
+    bs = [S.uneven_batch(6, seed=s, lo=3000, hi=20000) for s in (61, 62)]
+    dev = [{k: torch.from_numpy(b[k]).cuda() for k in ("x", "y", "layer", "weight")} for b in bs]
+    outs = [{k: torch.empty(int(b["offsets"][-1]), dtype=torch.float32 if k in ("rho", "delta") else torch.int32,
+                            device="cuda") for k in ("rho", "delta", "nearestHigher", "isSeed", "clusterIndex")}
+            for b in bs]
+    counts = []
+    for i in (0, 1, 0, 0, 0, 1, 1, 1):  # direct, direct, direct, capture, replay, direct, capture, replay
+        for v in outs[i].values():
+            v.zero_()
+        algo.run_batch(bs[i]["offsets"], dev[i]["x"], dev[i]["y"], dev[i]["layer"], dev[i]["weight"], out=outs[i],
+                       flags=C.DEVICE_MEMORY)
+        algo.synchronize()
+        counts.append(algo.last_run_stats()["kernel_launches"])
+        assert_bitexact({k: v.cpu().numpy() for k, v in outs[i].items()}, _oracle_batch(bs[i]))
+    assert counts[2:5] == [counts[0]] * 3 and counts[5:] == [counts[1]] * 3
+    algo.close()
