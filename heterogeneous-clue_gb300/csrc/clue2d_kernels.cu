@@ -38,6 +38,8 @@
 #include <cstdint>
 #include <cstring>
 
+#include <algorithm>
+
 #include "clue_internal.h"
 
 namespace clue {
@@ -1067,16 +1069,32 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   mark(3);
-  const bool two_class = t.big_threads > 0 && t.big_capacity > t.layer_capacity;
+  const int n_items = b.n_events * kLayers;
+  // No more layers than SMs (a single event): one pass of the widest CTA per
+  // layer, so that each layer's phases spread over 32 warps and large layers
+  // stay on chip.  Measured per producer call: 0.177 -> 0.131 ms on events of
+  // 150k-200k points, 0.136 -> 0.117 ms on 50k-150k, 0.113 -> 0.101 ms on 5k-20k.
+  Tuning2D tt = t;
   {
-    const int n_items = b.n_events * kLayers;
-    err = launch_layers_any(t.threads, b, p, t.layer_capacity, two_class ? t.layer_capacity : INT_MAX, 0,
-                            layer_grid(t, n_items), s);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (n_items <= sms) {
+      tt.threads = 1024;
+      tt.layer_capacity = std::max(std::max(t.layer_capacity, t.big_capacity), 4096);
+      tt.ctas_per_sm = 0;
+      tt.big_threads = tt.big_capacity = 0;
+    }
+  }
+  const bool two_class = tt.big_threads > 0 && tt.big_capacity > tt.layer_capacity;
+  {
+    err = launch_layers_any(tt.threads, b, p, tt.layer_capacity, two_class ? tt.layer_capacity : INT_MAX, 0,
+                            layer_grid(tt, n_items), s);
     if (err == cudaSuccess && two_class) {
       Tuning2D big;
-      big.threads = t.big_threads;
-      big.layer_capacity = t.big_capacity;
-      err = launch_layers_any(t.big_threads, b, p, t.big_capacity, INT_MAX, 1, layer_grid(big, n_items), s);
+      big.threads = tt.big_threads;
+      big.layer_capacity = tt.big_capacity;
+      err = launch_layers_any(tt.big_threads, b, p, tt.big_capacity, INT_MAX, 1, layer_grid(big, n_items), s);
     }
   }
   if (err != cudaSuccess) return err;
