@@ -45,11 +45,11 @@ PARAMS = (1.3, 2.0, 2.0)
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13.6M points);
 # traffic grows with the point count, so a full launch is scaled by its points.
-K_LAYERS_DRAM_BYTES_PER_POINT = 24.70
+K_LAYERS_DRAM_BYTES_PER_POINT = 24.77
 # Warp instructions per point of k_layers (both passes), same capture: the
 # kernel is bound by instruction issue, so its issue rate against the SMs'
 # peak (4 schedulers x 1 instruction per cycle) is the bound that applies.
-K_LAYERS_WARP_INST_PER_POINT = 96.3
+K_LAYERS_WARP_INST_PER_POINT = 96.5
 
 
 
