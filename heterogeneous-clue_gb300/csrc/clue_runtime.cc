@@ -119,7 +119,8 @@ enum Slot2D : int {
   S_OFF, S_CS, S_LCNT, S_LSTART, S_CURSOR, S_GX, S_GY, S_GW, S_GID,
   S_SP0, S_SP1, S_SP2, S_SP3, S_SP4, S_SP5, S_SP6, S_SP7,
   S_SPTBL, S_CSEED, S_CBASE, S_FLAGS, S_ORDER, S_CEV,
-  S_IN_X, S_IN_Y, S_IN_L, S_IN_W, S_OUT_RHO, S_OUT_DELTA, S_OUT_NH, S_OUT_SEED, S_OUT_CI,
+  S_IN,   // host runs: x | y | layer | w of the run, each N long, back to back
+  S_OUT,  // host runs: rho | delta | nearestHigher | isSeed | clusterIndex, likewise
   S_COUNT
 };
 
@@ -144,8 +145,8 @@ std::vector<size_t> sizes_2d(int32_t E, int64_t N, int64_t nchunks, int grid, bo
   s[S_FLAGS] = 4 * kFlagCount;
   s[S_ORDER] = 4 * ((size_t)E * kLayers + 2 * kSizeBuckets);
   if (host_io) {
-    s[S_IN_X] = s[S_IN_Y] = s[S_IN_L] = s[S_IN_W] = 4 * (size_t)N;
-    s[S_OUT_RHO] = s[S_OUT_DELTA] = s[S_OUT_NH] = s[S_OUT_SEED] = s[S_OUT_CI] = 4 * (size_t)N;
+    s[S_IN] = 16 * (size_t)N;
+    s[S_OUT] = 20 * (size_t)N;
   }
   return s;
 }
@@ -247,26 +248,57 @@ int enqueue_2d(Handle* h, const Run2D& r, Batch2D& b, bool host_io, cudaEvent_t*
                       4 * (size_t)b.n_chunks, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "H2D chunk events");
   if (host_io) {
-    if ((e = cudaMemcpyAsync((void*)b.x, r.x, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync((void*)b.y, r.y, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync((void*)b.layer, r.layer, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync((void*)b.w, r.w, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    // back-to-back host arrays (a server's staging) move in one copy
+    const char* hx = reinterpret_cast<const char*>(r.x);
+    if (reinterpret_cast<const char*>(r.y) == hx + n4 && reinterpret_cast<const char*>(r.layer) == hx + 2 * n4 &&
+        reinterpret_cast<const char*>(r.w) == hx + 3 * n4) {
+      if ((e = cudaMemcpyAsync((void*)b.x, r.x, 4 * n4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_error(e, "H2D points");
+    } else if ((e = cudaMemcpyAsync((void*)b.x, r.x, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync((void*)b.y, r.y, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync((void*)b.layer, r.layer, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync((void*)b.w, r.w, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
       return cuda_error(e, "H2D points");
+    }
   }
   e = launch_clue2d(b, h->p2d, h->tuning, s, stage_events, kernels);
   if (e != cudaSuccess) return cuda_error(e, "launching CLUE kernels");
   if (host_io) {
     const clue_outputs* o = r.out;
-    if ((e = cudaMemcpyAsync(o->rho, b.rho, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(o->delta, b.delta, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(o->nearestHigher, b.nh, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(o->isSeed, b.seed, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(o->clusterIndex, b.ci, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    const char* ho = reinterpret_cast<const char*>(o->rho);
+    if (reinterpret_cast<const char*>(o->delta) == ho + n4 &&
+        reinterpret_cast<const char*>(o->nearestHigher) == ho + 2 * n4 &&
+        reinterpret_cast<const char*>(o->isSeed) == ho + 3 * n4 &&
+        reinterpret_cast<const char*>(o->clusterIndex) == ho + 4 * n4) {
+      if ((e = cudaMemcpyAsync(o->rho, b.rho, 5 * n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_error(e, "D2H outputs");
+    } else if ((e = cudaMemcpyAsync(o->rho, b.rho, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(o->delta, b.delta, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(o->nearestHigher, b.nh, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(o->isSeed, b.seed, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(o->clusterIndex, b.ci, n4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
       return cuda_error(e, "D2H outputs");
+    }
   }
   e = cudaMemcpyAsync(h->flags_host.p, b.flags, 4 * kFlagCount, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_error(e, "D2H status");
   return CLUE_OK;
+}
+
+// Device inputs and outputs of a host-memory run of N points: each array N
+// long, back to back, so that back-to-back host arrays move in one copy.
+void host_io_views(void* in, void* out, int64_t N, Batch2D& b) {
+  float* fi = static_cast<float*>(in);
+  float* fo = static_cast<float*>(out);
+  b.x = fi;
+  b.y = fi + N;
+  b.layer = reinterpret_cast<const int32_t*>(fi + 2 * N);
+  b.w = fi + 3 * N;
+  b.rho = fo;
+  b.delta = fo + N;
+  b.nh = reinterpret_cast<int32_t*>(fo + 2 * N);
+  b.seed = reinterpret_cast<int32_t*>(fo + 3 * N);
+  b.ci = reinterpret_cast<int32_t*>(fo + 4 * N);
 }
 
 void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, Batch2D& b,
@@ -279,15 +311,7 @@ void fill_batch_views(Handle* h, const Run2D& r, int64_t nchunks, bool host_io, 
   b.offsets = static_cast<const int64_t*>(P(S_OFF));
   b.chunk_start = static_cast<const int32_t*>(P(S_CS));
   if (host_io) {
-    b.x = static_cast<const float*>(P(S_IN_X));
-    b.y = static_cast<const float*>(P(S_IN_Y));
-    b.layer = static_cast<const int32_t*>(P(S_IN_L));
-    b.w = static_cast<const float*>(P(S_IN_W));
-    b.rho = static_cast<float*>(P(S_OUT_RHO));
-    b.delta = static_cast<float*>(P(S_OUT_DELTA));
-    b.nh = static_cast<int32_t*>(P(S_OUT_NH));
-    b.seed = static_cast<int32_t*>(P(S_OUT_SEED));
-    b.ci = static_cast<int32_t*>(P(S_OUT_CI));
+    host_io_views(P(S_IN), P(S_OUT), r.N, b);
   } else {
     b.x = r.x;
     b.y = r.y;
@@ -432,7 +456,8 @@ int run_2d_plain(Handle* h, const Run2D& r) {
   const int grid = layer_grid_max(h->tuning, kLayers);
   auto need = sizes_2d(1, maxn, maxchunks, grid, false);
   if (host_io) {
-    for (int s = S_IN_X; s <= S_OUT_CI; ++s) need[s] = 4 * (size_t)maxn;
+    need[S_IN] = 16 * (size_t)maxn;
+    need[S_OUT] = 20 * (size_t)maxn;
   }
   need[S_OFF] = 16 * (size_t)std::max(r.E, 1);
   need[S_CS] = 8 * (size_t)std::max(r.E, 1);
@@ -474,15 +499,7 @@ int run_2d_plain(Handle* h, const Run2D& r) {
     b.chunk_start = static_cast<const int32_t*>(h->arena.ptr(S_CS)) + 2 * ev;
     const size_t n4 = 4 * (size_t)n;
     if (host_io) {
-      b.x = static_cast<const float*>(h->arena.ptr(S_IN_X));
-      b.y = static_cast<const float*>(h->arena.ptr(S_IN_Y));
-      b.layer = static_cast<const int32_t*>(h->arena.ptr(S_IN_L));
-      b.w = static_cast<const float*>(h->arena.ptr(S_IN_W));
-      b.rho = static_cast<float*>(h->arena.ptr(S_OUT_RHO));
-      b.delta = static_cast<float*>(h->arena.ptr(S_OUT_DELTA));
-      b.nh = static_cast<int32_t*>(h->arena.ptr(S_OUT_NH));
-      b.seed = static_cast<int32_t*>(h->arena.ptr(S_OUT_SEED));
-      b.ci = static_cast<int32_t*>(h->arena.ptr(S_OUT_CI));
+      host_io_views(h->arena.ptr(S_IN), h->arena.ptr(S_OUT), n, b);
       if ((e = cudaMemcpyAsync((void*)b.x, r.x + s0, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
           (e = cudaMemcpyAsync((void*)b.y, r.y + s0, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
           (e = cudaMemcpyAsync((void*)b.layer, r.layer + s0, n4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
