@@ -2,6 +2,7 @@
 // src/serial/plugin-CLUEClusterizer/CLUEAlgoKernels.h re-designed for the GPU.
 //
 // Pipeline of one batch (events concatenated in CSR order):
+//   k_init         the batch's counters, tickets and flags
 //   k_count        points per (event, layer), warp-aggregated atomics; also
 //                  notes whether every event is already grouped by layer
 //   k_layer_scan   per-event exclusive scan -> first position of each layer
@@ -585,6 +586,18 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
 }
 // ------------------------------------------------------------------ kernels
 
+// Per-batch counters to their start values: layer counts and per-chunk seed
+// counts to 0, the tickets and pass counters to 0, "grouped" to 1 (k_count
+// clears it on the first layer decrease).  The error word is left alone: it
+// accumulates over the launches of a run.
+__global__ void k_init(Batch2D b, int64_t n_lcnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n_lcnt) b.lcnt[i] = 0;
+  if (i < b.n_chunks) b.chunk_seeds[i] = 0;
+  if (i < kFlagCount - kFlagTicket) b.flags[kFlagTicket + i] = 0;
+  if (i == 0) b.flags[kFlagGrouped] = 1;
+}
+
 __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
   const int c = blockIdx.x;
   __shared__ int s_e;
@@ -1043,21 +1056,14 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
-  err = cudaMemsetAsync(b.lcnt, 0, sizeof(int32_t) * (size_t)b.n_events * kLayers, s);
-  if (err != cudaSuccess) return err;
-  // ticket and counters restart; the error word is left to the caller so
-  // that it can accumulate over several launches
-  err = cudaMemsetAsync(b.flags + kFlagTicket, 0, sizeof(int32_t) * (kFlagCount - kFlagTicket), s);
-  if (err != cudaSuccess) return err;
-  // grouped = 1 until k_count sees a layer decrease (low byte of a zeroed word)
-  err = cudaMemsetAsync(b.flags + kFlagGrouped, 0, sizeof(int32_t), s);
-  if (err != cudaSuccess) return err;
-  err = cudaMemsetAsync(b.flags + kFlagGrouped, 1, 1, s);
-  if (err != cudaSuccess) return err;
   const int nc = b.n_chunks;
-  // seeds per chunk are counted by k_layers as it flags them
-  err = cudaMemsetAsync(b.chunk_seeds, 0, sizeof(int32_t) * (size_t)nc, s);
-  if (err != cudaSuccess) return err;
+  {
+    // counters, tickets and flags of this batch (seeds per chunk are counted
+    // by k_layers as it flags them)
+    const int64_t n_lcnt = (int64_t)b.n_events * kLayers;
+    const int64_t n_init = std::max<int64_t>(std::max<int64_t>(n_lcnt, nc), kFlagCount);
+    k_init<<<(unsigned)((n_init + 255) / 256), 256, 0, s>>>(b, n_lcnt);
+  }
   const int warps_grid = (b.n_events * 32 + 255) / 256;
   mark(0);
   k_count<<<nc, kChunkThreads, 0, s>>>(b);
@@ -1105,7 +1111,7 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   mark(6);
   k_label<<<nc, kChunkThreads, 0, s>>>(b);
   mark(7);
-  if (kernels) *kernels += 7 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
+  if (kernels) *kernels += 8 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
   return cudaGetLastError();
 }
 
