@@ -6,8 +6,12 @@
 //   k_count        points per (event, layer), warp-aggregated atomics; also
 //                  notes whether every event is already grouped by layer
 //   k_layer_scan   per-event exclusive scan -> first position of each layer
+//                  (and, for batches of a few layers per CTA, layer sizes)
+//   k_order        those batches only: layers in descending size
 //   k_scatter      group points by (event, layer) when the input is not
-//   k_layers       persistent CTAs over the (event, layer) queue.  Per layer,
+//   k_layers       persistent CTAs over the (event, layer) queue (one wide
+//                  pass for a single event, else one or two classes of layer
+//                  size); the next layer's inputs prefetched into L2.  Per layer,
 //                  on-chip: counting sort into the reference's 5 cm tiles
 //                  (column-major, index order inside a tile), density,
 //                  nearest-higher, seed/outlier flags (and seeds counted per
