@@ -42,6 +42,19 @@ def max_ulp(a, b):
     return int(np.max(np.abs(a - b))) if a.size else 0
 
 
+def assert_bitexact_nan(got, want, keys=KEYS_2D, label=""):
+    """assert_bitexact, except that a NaN matches any NaN (the GPU returns
+    the canonical NaN, a CPU keeps the input's payload)."""
+    g2, w2 = {}, {}
+    for k in keys:
+        g, w = np.asarray(got[k]), np.asarray(want[k])
+        if g.dtype == np.float32:
+            both = np.isnan(g) & np.isnan(w)
+            g, w = np.where(both, np.float32(0), g), np.where(both, np.float32(0), w)
+        g2[k], w2[k] = g, w
+    assert_bitexact(g2, w2, keys, label)
+
+
 def assert_bitexact(got, want, keys=KEYS_2D, label=""):
     """Every output array identical bit for bit; on failure, report the first
     mismatches and the max ULP distance of the float arrays."""

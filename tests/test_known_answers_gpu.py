@@ -9,7 +9,7 @@ import pytest
 import clue_gb300 as C
 import oracle
 
-from _util import assert_bitexact
+from _util import assert_bitexact, assert_bitexact_nan
 
 pytestmark = pytest.mark.gpu
 FMAX = np.finfo(np.float32).max
@@ -98,3 +98,34 @@ def test_chain_to_an_outlier_stays_unassigned(run):
 def test_layers_never_interact(run):
     o = run([0.0, 0.0], [0.0, 0.0], [0, 99], [1.0, 1.0], 1.0, 0.5, 2.0)
     assert o["isSeed"].tolist() == [1, 1] and o["clusterIndex"].tolist() == [0, 1]
+
+
+def test_non_finite_inputs(cuda_lib):
+    """NaN and +-inf coordinates and weights against the oracle (which the
+    reference pins for NaN and -inf coordinates; a NaN rho has the reference
+    index followers[-1], where the oracle and the GPU keep -1)."""
+    from clue_gb300 import synthetic as S
+    ev = S.toy_event(6, blobs_per_layer=4, noise_per_layer=30)
+    rng = np.random.default_rng(4)
+    n = ev["x"].size
+    k = rng.choice(n, 120, replace=False)
+    ev["x"][k[:20]] = np.nan
+    ev["y"][k[20:35]] = np.nan
+    ev["x"][k[35:45]] = -np.inf
+    ev["y"][k[45:55]] = np.inf
+    ev["weight"][k[55:75]] = np.nan
+    ev["weight"][k[75:90]] = np.inf
+    ev["weight"][k[90:100]] = -np.inf
+    ev["x"][k[100:120]] = np.float32(3e9)
+    algo = C.Clusterizer(1.3, 2.0, 2.0)
+    try:
+        got = algo.make_clusters(ev["x"], ev["y"], ev["layer"], ev["weight"])
+        off = np.array([0, n, 2 * n], np.int64)
+        cat = {f: np.concatenate([ev[f], ev[f]]) for f in ("x", "y", "layer", "weight")}
+        both = algo.run_batch(off, cat["x"], cat["y"], cat["layer"], cat["weight"])
+    finally:
+        algo.close()
+    want = oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], 1.3, 2.0, 2.0)
+    assert_bitexact_nan(got, want, label="single event")
+    for e in range(2):
+        assert_bitexact_nan({f: v[e * n:(e + 1) * n] for f, v in both.items()}, want, label=f"batch event {e}")
