@@ -55,8 +55,9 @@ __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ int warp_id() { return threadIdx.x >> 5; }
 
 // LayerTilesSerial::getXBin / getYBin (src/serial/DataFormats/LayerTilesSerial.h:24-40):
-// (v - (-250)) * 0.2 in float, truncated toward zero (saturating, NaN -> 0),
-// clamped to [0, 99].
+// (v - (-250)) * 0.2 in float, truncated toward zero (saturating), clamped to
+// [0, 99]; a NaN lands in bin 0 (the conversion gives 0 or INT_MIN, both
+// clamped to 0), as (int)NaN does on the aarch64 host.
 __device__ __forceinline__ int tile_bin(float v) {
   const int b = __float2int_rz(__fmul_rn(__fsub_rn(v, -250.f), 0.2f));
   return min(max(b, 0), kGridCols - 1);

@@ -59,9 +59,13 @@ __device__ __forceinline__ int eta_bin(float eta, const Params3D& P) {
   return min(max(b, 0), kEtaBins - 1);
 }
 
-// TICLLayerTileT::phiBin (TICLLayerTile.h:28-34): (normPhi + M_PI) * r in double
+// TICLLayerTileT::phiBin (TICLLayerTile.h:28-34): (normPhi + M_PI) * r in double.
+// A NaN (phi NaN or +-inf, which reduce to NaN) takes bin 0: the reference's
+// int conversion is undefined there, 0 on the aarch64 host, and the device's
+// conversion would give INT_MIN.
 __device__ __forceinline__ int phi_bin(float phi, const Params3D& P) {
   const float norm = reduce_range(phi, P);
+  if (norm != norm) return 0;
   return __double2int_rz(__dmul_rn(__dadd_rn((double)norm, 3.14159265358979323846), (double)P.phi_r));
 }
 

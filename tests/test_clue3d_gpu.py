@@ -8,7 +8,7 @@ import clue_gb300 as C
 import oracle
 from clue_gb300 import synthetic as S
 
-from _util import KEYS_3D, assert_bitexact, golden_3d, load_golden_3d
+from _util import KEYS_3D, assert_bitexact, golden_3d, load_golden_3d, assert_bitexact_nan
 
 pytestmark = pytest.mark.gpu
 
@@ -88,3 +88,22 @@ def test_bad_layer_3d(algo):
     want, wnt = oracle.clue3d(ev)
     assert nt[0] == wnt
     assert_bitexact(_as_oracle(out), want, KEYS_3D)
+
+
+def test_non_finite_and_huge_phi_3d(algo):
+    """A phi that stays far outside [-pi, pi] after the reference's range
+    reduction (|phi| of 1e12 here) is rejected (the reference would index
+    outside its tile); NaN and +-inf phi reduce to NaN and take phi bin 0, as
+    in the oracle."""
+    ev = S.clue3d_event(9, n_clusters=500, n_layers=94)
+    ev["phi"][10] = np.float32(1e12)
+    with pytest.raises(C.ClueError) as ei:
+        algo.run_clue3d(np.array([0, 500], np.int64), ev)
+    assert ei.value.code == C.CLUE_EINVAL
+    ev["phi"][10] = np.nan
+    ev["phi"][11] = np.inf
+    ev["phi"][12] = -np.inf
+    out, nt = algo.run_clue3d(np.array([0, 500], np.int64), ev)
+    want, wnt = oracle.clue3d(ev)
+    assert nt[0] == wnt
+    assert_bitexact_nan(_as_oracle(out), want, KEYS_3D)
