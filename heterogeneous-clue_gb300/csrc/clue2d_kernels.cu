@@ -584,8 +584,9 @@ __device__ void process_layer(const Params2D& P, const LayerStore<TT, QT>& S, co
   }
   for (int q = tid; q < m; q += NT) {
     const int r = (int)root[q];
-    // seed roots carry their event-local index until k_seed_rank/k_label
-    b.ci[in.ev_start + S.rec[q].z] = (par[r] == -2) ? (int)S.rec[r].z : -1;
+    // a chain ending at a seed carries -(seed's event-local index + 2) until
+    // k_seed_rank (seeds) and k_label (the others) put the seed's rank there
+    b.ci[in.ev_start + S.rec[q].z] = (par[r] == -2) ? -((int)S.rec[r].z + 2) : -1;
   }
   __syncthreads();
 }
@@ -908,23 +909,28 @@ __global__ void __launch_bounds__(kChunkThreads) k_label(Batch2D b) {
   const int64_t i0 = es + (int64_t)(c - b.chunk_start[e]) * kChunk;
   const int64_t i1 = min(i0 + (int64_t)kChunk, ee);
   const int64_t n_ev = ee - es;
-  // v is the event-local index of the root seed (or -1); points with an
-  // invalid layer were never written, so v is range-checked.  The roots are
-  // seeds, which this kernel never writes; the gathers of one thread's points
-  // are issued together.
+  // ci holds a seed's rank (>= 0, from k_seed_rank), -1 (no cluster), or
+  // -(root + 2) for a point whose chain ends at the seed `root` (event-local
+  // index); only the last kind is rewritten, with the root's rank.  Points
+  // with an invalid layer were never written, so the root is range-checked.
+  // The roots are seeds, which this kernel never writes; the gathers of one
+  // thread's points are issued together.
   constexpr int PER = kChunk / kChunkThreads;
   int v[PER], r[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
-    v[j] = (i < i1 && !b.seed[i]) ? b.ci[i] : INT_MIN;
+    v[j] = i < i1 ? b.ci[i] : -1;
   }
 #pragma unroll
-  for (int j = 0; j < PER; ++j) r[j] = (v[j] >= 0 && v[j] < n_ev) ? b.ci[es + v[j]] : -1;
+  for (int j = 0; j < PER; ++j) {
+    const int64_t root = -(int64_t)v[j] - 2;
+    r[j] = (v[j] <= -2 && root < n_ev) ? b.ci[es + root] : -1;
+  }
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
-    if (v[j] != INT_MIN) b.ci[i] = r[j];
+    if (i < i1 && v[j] <= -2) b.ci[i] = r[j];
   }
 }
 
