@@ -107,3 +107,23 @@ def test_non_finite_and_huge_phi_3d(algo):
     want, wnt = oracle.clue3d(ev)
     assert nt[0] == wnt
     assert_bitexact_nan(_as_oracle(out), want, KEYS_3D)
+
+
+@pytest.mark.parametrize("prm", [{}, dict(density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)])
+def test_side_boundary_and_high_eta_3d(algo, prm):
+    """Dense clusters on layers 44-51 around the detector sides' split (94
+    layers: density windows stop below 47, the upper nearest-higher window
+    starts at 48), eta up to 3.0, phi in a narrow band (the event the CPU
+    tests pin on the reference)."""
+    rng = np.random.default_rng(11)
+    ev = S.clue3d_event(12, n_clusters=3000, n_layers=94, eta_range=(2.8, 3.0))
+    layer = rng.integers(44, 52, ev["z"].size).astype(np.int32)
+    phi = rng.uniform(0.0, 0.4, ev["z"].size).astype(np.float32)
+    z = S.layer_z(94)[layer].astype(np.float32)
+    r = ev["r_over_absz"] * z
+    ev.update(layer=layer, phi=phi, z=z, x=(r * np.cos(phi)).astype(np.float32), y=(r * np.sin(phi)).astype(np.float32))
+    n = ev["z"].size
+    out, nt = algo.run_clue3d(np.array([0, n], np.int64), ev, params=dict(n_layers=94, **prm))
+    want, wnt = oracle.clue3d(ev, **prm)
+    assert nt[0] == wnt
+    assert_bitexact(_as_oracle(out), want, KEYS_3D)

@@ -72,6 +72,26 @@ def test_oracle_matches_reference_3d_scintillator_and_wrap():
     assert_bitexact(got, want, KEYS_3D)
 
 
+@needs_ref
+@pytest.mark.parametrize("prm", [{}, dict(density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)])
+def test_oracle_3d_side_boundary_and_high_eta_on_the_reference(prm):
+    """Dense clusters on layers 44-51 only, around the detector sides' split
+    (density windows stop below layer 47, the upper nearest-higher window
+    starts at 48 with 94 layers), with eta up to 3.0 (the last eta rows) and
+    phi in a narrow band: every cluster's windows cross the boundary."""
+    rng = np.random.default_rng(11)
+    ev = S.clue3d_event(12, n_clusters=3000, n_layers=94, eta_range=(2.8, 3.0))
+    layer = rng.integers(44, 52, ev["z"].size).astype(np.int32)
+    phi = rng.uniform(0.0, 0.4, ev["z"].size).astype(np.float32)
+    z = S.layer_z(94)[layer].astype(np.float32)
+    r = ev["r_over_absz"] * z
+    ev.update(layer=layer, phi=phi, z=z, x=(r * np.cos(phi)).astype(np.float32), y=(r * np.sin(phi)).astype(np.float32))
+    got, nt = oracle.clue3d(ev, **prm)
+    want, nt2 = oracle.ref_clue3d(ev, **prm)
+    assert nt == nt2
+    assert_bitexact(got, want, KEYS_3D)
+
+
 def test_oracle_known_answers():
     """Hand-derived answers for a few micro cases."""
     # one point: rho = own weight, no higher, seed iff rho >= rhoc
