@@ -144,31 +144,56 @@ def cpu_sample(b, n_sample):
     return dict(offsets=off, **{k: np.concatenate(v) for k, v in parts.items()})
 
 
-def time_cpu(b, n_sample, threads):
+def cpu_kind():
+    """"reference" when the unmodified reference can be built here (from its
+    tree or its install under baseline/_ref), else "port"."""
+    import oracle
+    try:
+        oracle.ref_lib()
+        return "reference"
+    except Exception:
+        return "port"
+
+
+def time_cpu(b, n_sample, threads, kind="port"):
+    """CPU throughput on a strided sample of the workload: the reference's own
+    CLUEAlgoSerial::makeClusters (kind "reference", one algorithm object per
+    thread, timed around the makeClusters calls) or the oracle port (kind
+    "port", timed around the whole batch call)."""
     import oracle
     smp = cpu_sample(b, n_sample)
-    t0 = time.perf_counter()
-    oracle.clue2d_batch(smp["offsets"], smp["x"], smp["y"], smp["layer"], smp["weight"], *PARAMS,
-                        n_threads=threads)
-    dt = time.perf_counter() - t0
+    args = (smp["offsets"], smp["x"], smp["y"], smp["layer"], smp["weight"], *PARAMS)
+    if kind == "reference":
+        _, dt = oracle.ref_clue2d_batch(*args, n_threads=threads)
+    else:
+        t0 = time.perf_counter()
+        oracle.clue2d_batch(*args, n_threads=threads)
+        dt = time.perf_counter() - t0
     ev = smp["offsets"].size - 1
     return dict(events=ev, points=int(smp["offsets"][-1]), seconds=dt, events_per_s=ev / dt,
                 gpoints_per_s=smp["offsets"][-1] / dt / 1e9)
 
 
-def time_cpu_single(reps=3):
+def time_cpu_single(reps=3, kind="port"):
     """Single-thread latency of the CPU implementation on one toy-detector
     event (100k points) and one HGCAL-occupancy event (about 325k points):
     the best of ``reps`` runs, input generation excluded."""
+    import numpy as np
+
     import oracle
     from clue_gb300 import synthetic as S
     res = {}
     for name, ev in (("toy_100k", S.toy_event(12345)), ("hgcal_event", S.hgcal_event(1000))):
         best = float("inf")
+        off = np.array([0, ev["x"].size], np.int64)
         for _ in range(reps):
-            t0 = time.perf_counter()
-            oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *PARAMS)
-            best = min(best, time.perf_counter() - t0)
+            if kind == "reference":
+                _, dt = oracle.ref_clue2d_batch(off, ev["x"], ev["y"], ev["layer"], ev["weight"], *PARAMS)
+            else:
+                t0 = time.perf_counter()
+                oracle.clue2d(ev["x"], ev["y"], ev["layer"], ev["weight"], *PARAMS)
+                dt = time.perf_counter() - t0
+            best = min(best, dt)
         res[name] = {"points": int(ev["x"].size), "ms": 1000.0 * best}
     return res
 
@@ -179,11 +204,12 @@ def run_reference(args):
         return 0
     b = gen_workload(args, 0)
     threads = os.cpu_count() or 1
+    kind = cpu_kind()
     for _ in range(args.warmup):
-        time_cpu(b, max(8, args.cpu_sample // 8), threads)
+        time_cpu(b, max(8, args.cpu_sample // 8), threads, kind)
     secs, evs, pts = 0.0, 0, 0
     for _ in range(args.steps):
-        r = time_cpu(b, args.cpu_sample, threads)
+        r = time_cpu(b, args.cpu_sample, threads, kind)
         secs += r["seconds"]
         evs += r["events"]
         pts += r["points"]
@@ -196,7 +222,9 @@ def run_reference(args):
             "data": "synthetic (seeded HGCAL-like generator)",
             "config": _config(args, b),
             "gpoints_per_s": pts / secs / 1e9,
-            "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": kind, "sample": sample,
+                             "implementation": ("CLUEAlgoSerial::makeClusters, unmodified reference sources"
+                                                if kind == "reference" else "oracle port (C restatement)")},
             "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -291,28 +319,84 @@ def config2_leg(C, torch, stream, args):
         algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
 
     def timed(flags, warm, steps):
+        """Per-step times (ms, CUDA events on the stream) of ``steps`` steps after ``warm``."""
         for _ in range(warm):
             run(flags)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        ts = []
         for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             run(flags)
-        e1.record(stream)
-        torch.cuda.synchronize()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
         algo.synchronize()
-        return e0.elapsed_time(e1) / steps
+        return ts
 
-    ms_b = timed(0, 3, 3)
-    ms_p = timed(C.PLAIN, 1, 1)
+    steps = max(5, args.steps)
+    tb = timed(0, 3, steps)
+    tp = timed(C.PLAIN, 2, steps)
+    ms_b, ms_p = statistics.median(tb), statistics.median(tp)
     tuning = algo.get_tuning()
+    chain = None if args.no_chain else chain_leg(C, torch, stream, algo, off, dev, out, steps)
     algo.close()
     del dev, out
     torch.cuda.empty_cache()
-    return {"events": E, "points": N, "batched_events_per_s": E / (ms_b / 1000.0),
-            "batched_gpoints_per_s": N / (ms_b / 1000.0) / 1e9, "plain_events_per_s": E / (ms_p / 1000.0),
-            "batched_over_plain": ms_p / ms_b, "batched_ms_per_step": ms_b, "plain_ms_per_step": ms_p,
-            "tuning": tuning}
+    res = {"events": E, "points": N, "steps": steps, "batched_events_per_s": E / (ms_b / 1000.0),
+           "batched_gpoints_per_s": N / (ms_b / 1000.0) / 1e9, "plain_events_per_s": E / (ms_p / 1000.0),
+           "batched_over_plain": ms_p / ms_b,
+           "batched_over_plain_min_median_max": [min(tp) / max(tb), ms_p / ms_b, max(tp) / min(tb)],
+           "batched_ms_min_median_max": [min(tb), ms_b, max(tb)],
+           "plain_ms_min_median_max": [min(tp), ms_p, max(tp)], "tuning": tuning}
+    return res, chain
+
+
+def chain_leg(C, torch, stream, algo, off, dev, out, steps):
+    """CLUE3D on the layer clusters of the 1,000 HGCAL-occupancy events: CLUE
+    2D (device resident), the 2D -> 3D bridge on the device (layer clusters
+    from the 2D clusters), then batched CLUE3D (100 layers, +-2 sibling
+    layers, criticalDensity 0.5) on the bridge's output.  Events/s of the
+    chain and each stage's share; stage times are CUDA events on the stream,
+    which also cover the bridge's read of the per-event cluster counts."""
+    prm3 = dict(n_layers=100, density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)
+    out3 = None
+    E = off.size - 1
+
+    def step():
+        nonlocal out3
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        t0 = time.perf_counter()
+        ev[0].record(stream)
+        algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY)
+        ev[1].record(stream)
+        coff, lc = algo.layer_clusters(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out)
+        ev[2].record(stream)
+        n3 = int(coff[-1])
+        if out3 is None or out3["rho"].numel() != n3:
+            out3 = {k: torch.empty(n3, dtype=torch.float32 if k in ("rho", "delta_transverse") else torch.int32,
+                                   device="cuda")
+                    for k in ("rho", "delta_transverse", "delta_layers", "nh_layer", "nh_index", "isSeed",
+                              "tracksterIndex")}
+        algo.run_clue3d(coff, lc, params=prm3, flags=C.DEVICE_MEMORY, out=out3)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        algo.synchronize()
+        wall = (time.perf_counter() - t0) * 1000.0
+        return [ev[i].elapsed_time(ev[i + 1]) for i in range(3)], wall, n3
+
+    for _ in range(2):
+        step()
+    rows = [step() for _ in range(steps)]
+    tot = [sum(r[0]) for r in rows]
+    med = statistics.median(tot)
+    stage = {name: statistics.median([r[0][i] for r in rows]) for i, name in enumerate(("clue2d", "bridge", "clue3d"))}
+    wall = statistics.median([r[1] for r in rows])
+    return {"events": E, "layer_clusters": rows[-1][2], "steps": steps, "events_per_s": E / (med / 1000.0),
+            "ms_per_step": med, "wall_ms_per_step": wall, "stage_ms": stage,
+            "stage_share": {k: v / med for k, v in stage.items()},
+            "clue3d_params": prm3, "bridge": "energy = sum of weights, x/y weighted means, layer_z 320-520 cm, "
+                                             "radius 2 cm, isSilicon 1"}
 
 
 def clue3d_leg(C, torch, stream, args):
@@ -445,19 +529,23 @@ def run_gb300(args):
                          "frac": issue_achieved / issue_peak, "sm_mhz": mhz}
 
     # ---- plain: the same kernels, one event per launch sequence
-    plain = None
+    plain = plain_spread = None
     if not args.no_plain:
         run(C.PLAIN)
         torch.cuda.synchronize()
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        psteps = max(1, args.steps // 3)
-        p0.record(stream)
-        for _ in range(psteps):
+        pts_ms = []
+        for _ in range(max(3, args.steps // 3)):
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
             run(C.PLAIN)
-        p1.record(stream)
-        torch.cuda.synchronize()
-        pms = max_over_ranks(p0.elapsed_time(p1))
-        plain = ws * E * psteps / (pms / 1000.0)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            pts_ms.append(max_over_ranks(p0.elapsed_time(p1)))
+        pms = statistics.median(pts_ms)
+        plain = ws * E / (pms / 1000.0)
+        plain_spread = {"plain_ms_min_median_max": [min(pts_ms), pms, max(pts_ms)], "steps": len(pts_ms),
+                        "batched_over_plain_min_median_max": [min(pts_ms) / ms_step, pms / ms_step,
+                                                              max(pts_ms) / ms_step]}
 
     # ---- serving, before the e2e leg: run after it (which leaves 7.8 GB of pinned
     # buffers in torch's host cache), the servers' p99 at 2,000 events/s measured
@@ -540,29 +628,40 @@ def run_gb300(args):
         single = {"event": "toy-detector, 100,000 points", "host_memory_ms": host_ms,
                   "device_memory_ms": s0.elapsed_time(s1) / 20}
 
-    config2 = None
+    config2 = chain = None
     if rank == 0 and not args.no_config2:
-        config2 = config2_leg(C, torch, stream, args)
+        config2, chain = config2_leg(C, torch, stream, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        r = time_cpu(b, args.cpu_sample, threads)
-        cpu = {"value": r["events_per_s"], "unit": "events/s", "cores": threads, "kind": "port",
+        kind = cpu_kind()
+        r = time_cpu(b, args.cpu_sample, threads, kind)
+        cpu = {"value": r["events_per_s"], "unit": "events/s", "cores": threads, "kind": kind,
                "sample": f"{r['events']} events strided over the workload ({r['points']} points), "
                          f"{r['seconds']:.1f} s on {threads} threads",
-               "gpoints_per_s": r["gpoints_per_s"], "single_thread_latency": time_cpu_single()}
+               "gpoints_per_s": r["gpoints_per_s"], "single_thread_latency": time_cpu_single(kind=kind)}
+        if kind == "reference":
+            # the oracle port on the same sample, for comparison
+            rp = time_cpu(b, args.cpu_sample, threads, "port")
+            cpu["port"] = {"value": rp["events_per_s"], "unit": "events/s", "cores": threads,
+                           "seconds": rp["seconds"]}
 
     if rank == 0:
+        # the ratios and the end-to-end figure first: a truncated line still shows them
         line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded HGCAL-like generator)",
-                "config": _config(args, b), "gpoints_per_s": gpts,
+                "gpoints_per_s": gpts,
                 "plain_events_per_s": plain, "batched_over_plain": (value / plain) if plain else None,
-                "stage_ms": stage_ms, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "serving": serving, "clue3d": clue3d, "hgcal_1000": config2, "single_event": single,
-                "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
-                "tuning": t_main}
+                "plain_spread": plain_spread,
+                "hgcal_1000_batched_over_plain": (config2["batched_over_plain_min_median_max"]
+                                                  if config2 else None),
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": launches_per_step * args.steps,
+                "config": _config(args, b), "stage_ms": stage_ms,
+                "clue3d": clue3d, "clue3d_from_config2": chain, "hgcal_1000": config2,
+                "serving": serving, "single_event": single, "tuning": t_main}
         print(json.dumps(line), flush=True)
     algo.close()
     if ws > 1:
@@ -593,6 +692,8 @@ def main():
     ap.add_argument("--no-config2", action="store_true",
                     help="skip the batched-vs-plain measurement on HGCAL-occupancy events")
     ap.add_argument("--config2-events", type=int, default=1000)
+    ap.add_argument("--no-chain", action="store_true",
+                    help="skip CLUE 2D -> bridge -> CLUE3D on the HGCAL-occupancy events")
     ap.add_argument("--clue3d-events", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -99,7 +99,8 @@ class RunStats(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_int64), ("batches", ctypes.c_int64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("mean_batch_events", ctypes.c_double),
-                ("max_inflight_seen", ctypes.c_double), ("slot_capacity_points", ctypes.c_int64)]
+                ("max_inflight_seen", ctypes.c_double), ("slot_capacity_points", ctypes.c_int64),
+                ("memory_waits", ctypes.c_int64)]
 
 
 def header_symbols():

@@ -971,7 +971,19 @@ cudaError_t prepare_clue2d_kernels(int device) {
   if ((e = allow_max_smem<128>(optin)) != cudaSuccess) return e;
   if ((e = allow_max_smem<256>(optin)) != cudaSuccess) return e;
   if ((e = allow_max_smem<512>(optin)) != cudaSuccess) return e;
-  return allow_max_smem<1024>(optin);
+  if ((e = allow_max_smem<1024>(optin)) != cudaSuccess) return e;
+  // Asking for a kernel's attributes loads its code on this device (the
+  // runtime loads kernels lazily, at first use, by default), so that no
+  // later launch of the pipeline has code to load.
+  const void* rest[] = {reinterpret_cast<const void*>(k_init), reinterpret_cast<const void*>(k_count),
+                        reinterpret_cast<const void*>(k_layer_scan), reinterpret_cast<const void*>(k_order),
+                        reinterpret_cast<const void*>(k_scatter), reinterpret_cast<const void*>(k_seed_chunk_scan),
+                        reinterpret_cast<const void*>(k_seed_rank), reinterpret_cast<const void*>(k_label)};
+  for (const void* f : rest) {
+    cudaFuncAttributes a;
+    if ((e = cudaFuncGetAttributes(&a, f)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 float sqrt_le_threshold(float d) {
@@ -1046,7 +1058,7 @@ int layer_grid(const Tuning2D& t, int n_items) {
     per_sm = per_sm < 1 ? 1 : per_sm;
   }
   int g = sms * per_sm;
-  if (g > n_items) g = n_items;
+  if (g > n_items) g = n_items;  // never more CTAs than (event, layer) items: see launch_clue2d
   return g < 1 ? 1 : g;
 }
 
@@ -1073,16 +1085,26 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
     // by k_layers as it flags them)
     const int64_t n_lcnt = (int64_t)b.n_events * kLayers;
     const int64_t n_init = std::max<int64_t>(std::max<int64_t>(n_lcnt, nc), kFlagCount);
+    NvtxRange r("clue2d/init");
     k_init<<<(unsigned)((n_init + 255) / 256), 256, 0, s>>>(b, n_lcnt);
   }
   const int warps_grid = (b.n_events * 32 + 255) / 256;
   mark(0);
-  k_count<<<nc, kChunkThreads, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/count");
+    k_count<<<nc, kChunkThreads, 0, s>>>(b);
+  }
   mark(1);
-  k_layer_scan<<<warps_grid, 256, 0, s>>>(b);
-  if (b.use_order) k_order<<<warps_grid, kSizeBuckets, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/layer_scan");
+    k_layer_scan<<<warps_grid, 256, 0, s>>>(b);
+    if (b.use_order) k_order<<<warps_grid, kSizeBuckets, 0, s>>>(b);
+  }
   mark(2);
-  k_scatter<<<nc, kChunkThreads, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/scatter");
+    k_scatter<<<nc, kChunkThreads, 0, s>>>(b);
+  }
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   mark(3);
@@ -1104,7 +1126,12 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
     }
   }
   const bool two_class = tt.big_threads > 0 && tt.big_capacity > tt.layer_capacity;
+  // Invariant: every layer-kernel grid is at most n_items = n_events * kLayers
+  // (layer_grid caps it there).  The per-CTA HBM tile tables of the spill
+  // path are sized on it: one table per (event, layer) at most, e.g. 100 for
+  // a single event, which the allocation-free entry point relies on.
   {
+    NvtxRange r("clue2d/layers");
     err = launch_layers_any(tt.threads, b, p, tt.layer_capacity, two_class ? tt.layer_capacity : INT_MAX, 0,
                             layer_grid(tt, n_items), s);
     if (err == cudaSuccess && two_class) {
@@ -1116,11 +1143,20 @@ cudaError_t launch_clue2d(const Batch2D& batch, const Params2D& p, const Tuning2
   }
   if (err != cudaSuccess) return err;
   mark(4);
-  k_seed_chunk_scan<<<warps_grid, 256, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/seed_chunk_scan");
+    k_seed_chunk_scan<<<warps_grid, 256, 0, s>>>(b);
+  }
   mark(5);
-  k_seed_rank<<<nc, kChunkThreads, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/seed_rank");
+    k_seed_rank<<<nc, kChunkThreads, 0, s>>>(b);
+  }
   mark(6);
-  k_label<<<nc, kChunkThreads, 0, s>>>(b);
+  {
+    NvtxRange r("clue2d/label");
+    k_label<<<nc, kChunkThreads, 0, s>>>(b);
+  }
   mark(7);
   if (kernels) *kernels += 8 + (b.use_order ? 1 : 0) + (two_class ? 1 : 0);
   return cudaGetLastError();

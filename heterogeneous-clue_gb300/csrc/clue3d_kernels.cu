@@ -432,14 +432,38 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   if (err != cudaSuccess) return err;
   const int T = 256;
   const int grid = (int)((b.n_points + T - 1) / T);
-  k3_key<<<grid, T, 0, s>>>(b, p);
-  k3_row_scan<<<b.n_events, 256, 0, s>>>(b);
-  k3_scatter<<<grid, T, 0, s>>>(b);
-  k3_row_sort<<<grid, T, 0, s>>>(b);
-  k3_density<<<grid, T, 0, s>>>(b, p);
-  k3_nh<<<grid, T, 0, s>>>(b, p);
-  k3_flags<<<grid, T, 0, s>>>(b, p);
-  k3_finish<<<b.n_events, 512, 0, s>>>(b);
+  {
+    NvtxRange r("clue3d/key");
+    k3_key<<<grid, T, 0, s>>>(b, p);
+  }
+  {
+    NvtxRange r("clue3d/row_scan");
+    k3_row_scan<<<b.n_events, 256, 0, s>>>(b);
+  }
+  {
+    NvtxRange r("clue3d/scatter");
+    k3_scatter<<<grid, T, 0, s>>>(b);
+  }
+  {
+    NvtxRange r("clue3d/row_sort");
+    k3_row_sort<<<grid, T, 0, s>>>(b);
+  }
+  {
+    NvtxRange r("clue3d/density");
+    k3_density<<<grid, T, 0, s>>>(b, p);
+  }
+  {
+    NvtxRange r("clue3d/nearest_higher");
+    k3_nh<<<grid, T, 0, s>>>(b, p);
+  }
+  {
+    NvtxRange r("clue3d/flags");
+    k3_flags<<<grid, T, 0, s>>>(b, p);
+  }
+  {
+    NvtxRange r("clue3d/finish");
+    k3_finish<<<b.n_events, 512, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 

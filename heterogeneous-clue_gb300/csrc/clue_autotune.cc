@@ -1,9 +1,10 @@
 // Autotuner of the batched CLUE 2D kernels (no reference counterpart).
 //
-// The knobs change only the work decomposition: threads per CTA, how many
+// The knobs change only the work decomposition: threads per CTA and how many
 // points of a layer stay on-chip (which sets CTAs per SM through shared
-// memory), and the query grouping tile inside the reference's 5 cm tiles.
-// Candidate enumeration order never changes, so every candidate must give
+// memory), for the first pass over the layers and for the second pass that
+// takes the layers above the first pass's capacity.  No knob changes which
+// candidates are summed or in what order, so every candidate must give
 // bit-identical outputs; the tuner checks that with a device-side digest
 // of all five output arrays and fails loudly when one differs.
 #include <cuda_runtime.h>

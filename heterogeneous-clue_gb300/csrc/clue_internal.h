@@ -2,11 +2,23 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstddef>
 #include <cstdint>
 
 namespace clue {
+
+// NVTX range over a scope: marks where each pipeline stage is queued on the
+// host timeline (Nsight Systems / Nsight Compute NVTX filters).  Inside a
+// stream capture the ranges mark the capture; a graph replay is one range.
+// With no tool attached a range costs a few nanoseconds.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Tile grid of the reference (src/serial/DataFormats/LayerTilesConstants.h:7-26):
 // 100 layers, x and y in [-250, 250] cm, 5 cm tiles -> 100 x 100 per layer.
@@ -100,8 +112,9 @@ int layer_grid(const Tuning2D& t, int n_items);
 int layer_grid_max(const Tuning2D& t, int n_items);
 size_t layer_smem_bytes(const Tuning2D& t);
 
-// Opts the layer kernels into the device's full shared memory (once per
-// device, outside any stream capture).
+// Opts the layer kernels into the device's full shared memory and loads the
+// code of every kernel of the 2D pipeline on the current device (outside any
+// stream capture; again after the device's context was reset).
 cudaError_t prepare_clue2d_kernels(int device);
 
 constexpr int kStages2D = 7;

@@ -6,14 +6,21 @@
 // code paths that run while another component owns the device's memory
 // management.  For them this entry point takes device pointers for inputs and
 // outputs and does all of its work in one fixed scratch area that is part of
-// the library image: a file-scope __device__ array, created when the library
-// is loaded on a device and kept until the process exits.
+// the library image: a file-scope __device__ array.
 //
 // Limits and rules (also in include/clue.h):
 //  * at most kNoAllocMaxPoints points per call; larger events get CLUE_EINVAL;
-//  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make
-//    that first call before any stream capture;
+//  * the runtime loads a library's device code, and creates its __device__
+//    arrays, lazily: on a device, the first use of this file's code creates
+//    the 14 MB array, and the first launch of each kernel loads its code.
+//    Make the first call on each device at start-up, before the caller's
+//    framework reserves the device's memory for its pool; a call with n == 0
+//    does exactly that set-up (array, kernel code, shared-memory opt-in)
+//    and nothing else.  Make it outside any stream capture.  The array then
+//    stays until the process exits;
+//  * every call looks the array's device address up again (cheap once the
+//    code is loaded), so a reset of the device's context in between does not
+//    leave a stale address behind;
 //  * every call on a device uses the same array: calls that overlap on the
 //    GPU (other streams or threads) race and corrupt each other; the call
 //    synchronises its stream before it returns;
@@ -23,7 +30,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "../../include/clue.h"
 #include "clue_internal.h"
@@ -33,7 +39,9 @@ namespace clue {
 namespace {
 
 constexpr int64_t kNoAllocMaxPoints = 1 << 18;  // 262,144 points per event
-constexpr int kNoAllocMaxGrid = kLayers;        // one CTA per layer at most
+// Per-CTA HBM tile tables of the spill path: launch_clue2d never launches more
+// layer-kernel CTAs than (event, layer) items, i.e. 100 for one event.
+constexpr int kNoAllocMaxGrid = kLayers;
 constexpr int64_t kNoAllocMaxChunks = kNoAllocMaxPoints / kChunk + 1;
 
 // Byte layout of the scratch area (every piece 256-byte aligned).
@@ -65,23 +73,22 @@ __global__ void k_noalloc_event_header(int64_t* offsets, int32_t* chunk_start, i
   chunk_start[1] = (int32_t)((n + kChunk - 1) / kChunk);
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
-
-// Per-device set-up: the device address of the scratch area (device current).
-int noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= kMaxDevices) return set_error(CLUE_EINVAL, "device %d out of range", device);
-  std::lock_guard<std::mutex> g(g_setup_mu);
-  if (!g_scratch_addr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(scratch)");
-    e = prepare_clue2d_kernels(device);
-    if (e != cudaSuccess) return cuda_error(e, "preparing kernels");
-    g_scratch_addr[device] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_addr[device];
+// Set-up on the current device: the scratch area's device address (looked
+// up on every call: cheap once the code is loaded, and never stale after a
+// context reset) and the kernels' code and shared-memory opt-in.
+int noalloc_scratch(unsigned char** out) {
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(scratch)");
+  cudaFuncAttributes a;
+  e = cudaFuncGetAttributes(&a, k_noalloc_event_header);
+  if (e != cudaSuccess) return cuda_error(e, "loading kernels");
+  e = prepare_clue2d_kernels(device);
+  if (e != cudaSuccess) return cuda_error(e, "preparing kernels");
+  *out = static_cast<unsigned char*>(p);
   return CLUE_OK;
 }
 
@@ -93,20 +100,20 @@ using namespace clue;
 extern "C" int clue_run_event_noalloc(const clue_params* params, int32_t n, const float* x, const float* y,
                                       const int32_t* layer, const float* weight, const clue_outputs* out,
                                       void* cuda_stream) {
-  if (!params || !out || !out->rho || !out->delta || !out->nearestHigher || !out->isSeed || !out->clusterIndex)
-    return set_error(CLUE_EINVAL, "NULL argument");
   if (n < 0) return set_error(CLUE_EINVAL, "n < 0");
   if (n > kNoAllocMaxPoints)
     return set_error(CLUE_EINVAL, "clue_run_event_noalloc: %d points exceed its fixed scratch (at most %lld)", n,
                      (long long)kNoAllocMaxPoints);
-  if (n == 0) return CLUE_OK;
-  if (!x || !y || !layer || !weight) return set_error(CLUE_EINVAL, "NULL input array");
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (n > 0) {
+    if (!params || !out || !out->rho || !out->delta || !out->nearestHigher || !out->isSeed || !out->clusterIndex)
+      return set_error(CLUE_EINVAL, "NULL argument");
+    if (!x || !y || !layer || !weight) return set_error(CLUE_EINVAL, "NULL input array");
+  }
   unsigned char* base = nullptr;
-  int rc = noalloc_scratch(device, &base);
+  int rc = noalloc_scratch(&base);
   if (rc) return rc;
+  if (n == 0) return CLUE_OK;  // the warm-up call: set-up only, every pointer may be NULL
+  cudaError_t e;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
 
   Batch2D b;
@@ -140,10 +147,9 @@ extern "C" int clue_run_event_noalloc(const clue_params* params, int32_t n, cons
   b.sp[0] = reinterpret_cast<float*>(base + kOffSpRec);
   b.sp[4] = reinterpret_cast<float*>(base + kOffSpNh);
   b.sp[5] = reinterpret_cast<float*>(base + kOffSpQord);
-  b.sp_tbl = reinterpret_cast<int32_t*>(base + kOffSpTbl);
+  b.sp_tbl = reinterpret_cast<int32_t*>(base + kOffSpTbl);  // kNoAllocMaxGrid tables: see its definition
 
-  Tuning2D t;  // the default decomposition; its grid never exceeds one CTA per layer
-  if (layer_grid(t, kLayers) > kNoAllocMaxGrid) return set_error(CLUE_ECUDA, "unexpected layer grid");
+  Tuning2D t;  // the default decomposition
   const Params2D p = make_params2d(params->dc, params->rhoc, params->outlierDeltaFactor);
 
   k_noalloc_event_header<<<1, 1, 0, s>>>(const_cast<int64_t*>(b.offsets), const_cast<int32_t*>(b.chunk_start), n);

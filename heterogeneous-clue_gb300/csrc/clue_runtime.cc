@@ -95,6 +95,16 @@ int DeviceArena::reserve(const std::vector<size_t>& need_in, size_t budget) {
   return CLUE_OK;
 }
 
+size_t DeviceArena::bytes_after(const std::vector<size_t>& need) const {
+  size_t t = 0;
+  for (size_t i = 0; i < need.size(); ++i) {
+    const size_t have = i < bufs_.size() ? bufs_[i].bytes : 0;
+    t += std::max((need[i] + 255) & ~size_t(255), have);
+  }
+  for (size_t i = need.size(); i < bufs_.size(); ++i) t += bufs_[i].bytes;
+  return t;
+}
+
 PinnedBuf::~PinnedBuf() {
   if (p) cudaFreeHost(p);
 }
@@ -176,6 +186,11 @@ int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io) {
   if (!rc) rc = h->stage.reserve(24 * (size_t)(E + 1) + 4 * (size_t)nchunks);
   if (!rc) rc = h->flags_host.reserve(4 * kFlagCount);
   return rc;
+}
+
+size_t arena_bytes_after_2d(const Handle* h, int32_t E, int64_t N, int64_t nchunks, bool host_io) {
+  const int grid = layer_grid_max(h->tuning, std::max(1, E * kLayers));
+  return h->arena.bytes_after(sizes_2d(E, N, nchunks, grid, host_io));
 }
 
 Handle::~Handle() {
@@ -423,6 +438,7 @@ int run_2d_batched(Handle* h, const Run2D& r, cudaEvent_t* stage_events = nullpt
       }
       h->graph_key = key;
     }
+    NvtxRange nr("clue2d/graph_replay");
     e = cudaGraphLaunch(h->graph_exec, h->stream);
     if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
     kernels = h->graph_kernels;

@@ -38,6 +38,9 @@ class DeviceArena {
  public:
   ~DeviceArena();
   int reserve(const std::vector<size_t>& need, size_t budget);
+  // Device bytes the arena would hold after reserve(need) without the growth
+  // margin (the margin is only taken when the budget has room for it).
+  size_t bytes_after(const std::vector<size_t>& need) const;
   void* ptr(int slot) const { return slot < (int)bufs_.size() ? bufs_[slot].p : nullptr; }
   size_t total() const { return total_; }
   uint64_t generation() const { return gen_; }  // bumped whenever a buffer is (re)allocated
@@ -89,6 +92,9 @@ struct Handle;
 // time (a server slot does this at start so that its first batches do not
 // allocate).
 int reserve_2d(Handle* h, int32_t E, int64_t N, bool host_io);
+// Device bytes the handle's 2D arena would hold after sizing it for a batch of
+// E events, N points and nchunks chunks (the batch's own chunk count).
+size_t arena_bytes_after_2d(const Handle* h, int32_t E, int64_t N, int64_t nchunks, bool host_io);
 
 // Internal run flag: host (pinned) buffers, but return once the work is
 // queued; completion is seen through Handle::done_event.  Used by the server.

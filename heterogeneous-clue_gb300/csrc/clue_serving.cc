@@ -4,15 +4,23 @@
 //
 // Requests are queued by clue_server_submit (inputs copied on submit).  A
 // scheduler thread owns `max_inflight` slots; each slot is a CLUE handle with
-// its own CUDA stream, resident device buffers and pinned staging, sized to
-// an equal share of the device-memory budget.  Whenever a slot is free and
-// requests are waiting, the scheduler admits as many queued events as fit
-// the slot (points and event count), stages them, and launches the batched
-// pipeline asynchronously; batches of different slots overlap on the device
-// (one batch's copies with another's kernels).  Completed batches are found
-// with cudaEventQuery (every 20 us while batches are in flight), their outputs
-// are copied to each caller's buffers, and the request latency (submit ->
-// outputs written) is recorded.  Host copies run on a resident pool.
+// its own CUDA stream, resident device buffers and pinned staging.  At start
+// every slot sizes its buffers for batches of up to 8M points within half of
+// an equal share of the budget, so that ordinary loads never allocate.
+// Whenever a slot is free and requests are waiting, the scheduler admits as
+// many queued events as fit those buffers (points and event count), stages
+// them, and launches the batched pipeline asynchronously; batches of different
+// slots overlap on the device (one batch's copies with another's kernels).
+// An event larger than a start-up batch goes alone and may take the rest of
+// the shared budget: it is admitted when the slots' device memory together
+// stays within the budget -- idle slots first give back what they grew beyond
+// their start-up buffers -- and otherwise waits, at the head of the queue,
+// until in-flight batches finish.  Only an event that cannot fit even when
+// every other slot holds just its start-up buffers is refused (CLUE_ENOMEM).
+// Completed batches are found with cudaEventQuery (every 20 us while batches
+// are in flight), their outputs are copied to each caller's buffers, and the
+// request latency (submit -> outputs written) is recorded.  Host copies run
+// on a resident pool.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -55,8 +63,8 @@ struct Slot {
   std::vector<Request*> reqs;
   bool busy = false;      // requests taken (staging, on the device or delivering results)
   bool launched = false;  // the batch is queued on the device
-  int64_t cap_points = 0;    // largest batch the slot's share of the budget holds
   int64_t batch_points = 0;  // batches are cut at this size: the buffers sized at start
+  size_t base_bytes = 0;     // device bytes of those start-up buffers
 };
 
 class Server {
@@ -68,33 +76,45 @@ class Server {
     if (cfg_.max_inflight < 1) cfg_.max_inflight = 1;
     if (cfg_.max_batch_events < 1) cfg_.max_batch_events = 1;
     if (!cfg_.device_budget_bytes) cfg_.device_budget_bytes = size_t(16) << 30;
-    const size_t share = cfg_.device_budget_bytes / cfg_.max_inflight;
+    budget_ = cfg_.device_budget_bytes;
+    // start-up buffers within half of an equal share: the other half of the
+    // budget stays free for events larger than a start-up batch
+    const size_t base_share = budget_ / (2 * (size_t)cfg_.max_inflight);
     slots_.resize(cfg_.max_inflight);
     for (auto& s : slots_) {
-      int rc = clue_create(&params_, share, cfg_.device, nullptr, &s.h);
+      int rc = clue_create(&params_, budget_, cfg_.device, nullptr, &s.h);
       if (rc) return rc;
       Handle* hh = reinterpret_cast<Handle*>(s.h);
-      // largest point count whose batch fits this slot's share
+      // largest batch (point count) whose buffers fit the start-up share
       int64_t lo = 0, hi = int64_t(1) << 31;
-      const int grid = layer_grid(hh->tuning, cfg_.max_batch_events * kLayers);
+      const int grid = layer_grid_max(hh->tuning, cfg_.max_batch_events * kLayers);
       while (hi - lo > 1) {
         const int64_t mid = (lo + hi) / 2;
         const int64_t chunks = mid / kChunk + cfg_.max_batch_events;
-        if (required_bytes_2d(cfg_.max_batch_events, mid, chunks, grid, true) <= share) lo = mid; else hi = mid;
+        if (required_bytes_2d(cfg_.max_batch_events, mid, chunks, grid, true) <= base_share) lo = mid; else hi = mid;
       }
-      s.cap_points = lo;
-      if (s.cap_points < 1) return set_error(CLUE_ENOMEM, "budget too small for one in-flight batch");
+      if (lo < 1) return set_error(CLUE_ENOMEM, "budget too small for one in-flight batch");
       // resident buffers for batches up to 8M points, so that ordinary loads
       // never allocate (and never synchronise the device) on the serving path
-      const int64_t pre = std::min<int64_t>(s.cap_points, int64_t(8) << 20);
-      s.batch_points = pre;
+      s.batch_points = std::min<int64_t>(lo, int64_t(8) << 20);
       cudaSetDevice(cfg_.device);
-      rc = reserve_2d(hh, cfg_.max_batch_events, pre, true);
-      if (!rc) rc = s.in.reserve(16 * (size_t)pre);
-      if (!rc) rc = s.out.reserve(20 * (size_t)pre);
+      rc = reserve_2d(hh, cfg_.max_batch_events, s.batch_points, true);
+      if (!rc) rc = s.in.reserve(16 * (size_t)s.batch_points);
+      if (!rc) rc = s.out.reserve(20 * (size_t)s.batch_points);
       if (rc) return rc;
+      s.base_bytes = hh->arena.total();
     }
-    cap_points_ = slots_[0].cap_points;
+    // the largest single event ever admitted: it fits the budget while every
+    // other slot holds only its start-up buffers
+    const size_t others = (slots_.size() - 1) * slots_[0].base_bytes;
+    const size_t room = budget_ > others ? budget_ - others : 0;
+    const Handle* h0 = reinterpret_cast<const Handle*>(slots_[0].h);
+    int64_t lo = 0, hi = int64_t(1) << 31;
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) / 2;
+      if (arena_bytes_after_2d(h0, 1, mid, mid / kChunk + 1, true) <= room) lo = mid; else hi = mid;
+    }
+    cap_points_ = lo;
     // helpers on all cores but two (the scheduler and a submitting client), at most 15
     pool_.start((int)std::min(15u, std::max(3u, std::thread::hardware_concurrency()) - 2));
     worker_ = std::thread([this] { loop(); });
@@ -134,7 +154,9 @@ class Server {
       if (n < 0 || n > INT32_MAX) return set_error(CLUE_EINVAL, "bad event_offsets");
       if (n > 0 && (!x || !y || !layer || !w)) return set_error(CLUE_EINVAL, "bad argument");
       if (n > cap_points_)
-        return set_error(CLUE_ENOMEM, "event of %lld points exceeds one in-flight batch (%lld points)",
+        return set_error(CLUE_ENOMEM,
+                         "event of %lld points exceeds what the device budget admits (%lld points with the other "
+                         "slots at their start-up buffers)",
                          (long long)n, (long long)cap_points_);
     }
     std::vector<Request*> rs(E);
@@ -227,6 +249,7 @@ class Server {
     st->mean_batch_events = batches_ ? double(batched_events_) / batches_ : 0.0;
     st->max_inflight_seen = max_inflight_seen_;
     st->slot_capacity_points = cap_points_;
+    st->memory_waits = memory_waits_;
   }
 
   void reset_stats() {
@@ -235,9 +258,17 @@ class Server {
     batches_ = 0;
     batched_events_ = 0;
     max_inflight_seen_ = 0;
+    memory_waits_ = 0;
   }
 
  private:
+  size_t others_bytes(const Slot& s) const {
+    size_t t = 0;
+    for (const auto& o : slots_)
+      if (&o != &s) t += reinterpret_cast<const Handle*>(o.h)->arena.total();
+    return t;
+  }
+
   // Completes every finished slot.  Called with mu_ held; the result copies
   // run with the lock released (only this thread touches slots), and the
   // statuses are published under the lock afterwards.
@@ -300,23 +331,55 @@ class Server {
   // Admits queued requests into a free slot and launches it.  Called with mu_
   // held; the requests are taken (and the slot marked busy, so that drain()
   // keeps waiting) under the lock, the staging copies and the launch run
-  // without it.
-  void admit(Slot& s, std::unique_lock<std::mutex>& g) {
+  // without it.  Returns false when the head of the queue waits for device
+  // memory (nothing is taken then).
+  bool admit(Slot& s, std::unique_lock<std::mutex>& g) {
     s.reqs.clear();
     s.off.assign(1, 0);
-    int64_t pts = 0;
+    int64_t pts = 0, nchunks = 0;
     while (!queue_.empty() && (int)s.reqs.size() < cfg_.max_batch_events) {
       Request* r = queue_.front();
       // batches stay within the buffers sized at start (a single larger event
-      // still goes, alone, and grows them once)
+      // still goes, alone)
       if (pts + r->n > s.batch_points && !s.reqs.empty()) break;
       queue_.pop_front();
       s.reqs.push_back(r);
       pts += r->n;
+      nchunks += (r->n + kChunk - 1) / kChunk;
       s.off.push_back(pts);
     }
     const int32_t E = (int32_t)s.reqs.size();
-    if (E == 0) return;
+    if (E == 0) return true;
+    Handle* hs = reinterpret_cast<Handle*>(s.h);
+    // device memory of all slots together stays within the budget
+    const size_t need = arena_bytes_after_2d(hs, E, pts, nchunks, true);
+    size_t others = others_bytes(s);
+    if (need + others > budget_) {
+      // idle slots give back what they grew beyond their start-up buffers
+      g.unlock();
+      for (auto& o : slots_) {
+        Handle* ho = reinterpret_cast<Handle*>(o.h);
+        if (&o == &s || o.busy || ho->arena.total() <= o.base_bytes) continue;
+        ho->arena.release();
+        ho->budget = budget_;
+        reserve_2d(ho, cfg_.max_batch_events, o.batch_points, true);
+        o.base_bytes = ho->arena.total();
+      }
+      g.lock();
+      others = others_bytes(s);
+      if (need + others > budget_) {
+        // the batch waits, in queue order, until in-flight batches finish
+        for (int32_t k = E - 1; k >= 0; --k) queue_.push_front(s.reqs[k]);
+        if (queue_.front()->id != waiting_id_) {
+          waiting_id_ = queue_.front()->id;
+          ++memory_waits_;
+        }
+        s.reqs.clear();
+        s.off.assign(1, 0);
+        return false;
+      }
+    }
+    hs->budget = budget_ - others;  // the room this slot may grow into
     s.busy = true;
     g.unlock();
     int rc = s.in.reserve(16 * (size_t)std::max<int64_t>(pts, 1));
@@ -362,7 +425,7 @@ class Server {
       s.reqs.clear();
       s.busy = false;
       done_cv_.notify_all();
-      return;
+      return true;
     }
     s.launched = true;
     ++batches_;
@@ -370,6 +433,7 @@ class Server {
     int inflight = 0;
     for (auto& t : slots_) inflight += t.busy;
     max_inflight_seen_ = std::max<double>(max_inflight_seen_, inflight);
+    return true;
   }
 
   void loop() {
@@ -384,8 +448,9 @@ class Server {
         busy |= s.busy;
       }
       if (free_slot && !queue_.empty()) {
-        admit(*free_slot, g);
-        continue;
+        if (admit(*free_slot, g)) continue;
+        // the head of the queue waits for device memory: a batch in flight
+        // holds it, so look again once batches have been reaped
       }
       if (busy) {
         // batches in flight: look again shortly (new arrivals wake us earlier)
@@ -406,7 +471,10 @@ class Server {
   clue_params params_;
   clue_server_config cfg_;
   std::vector<Slot> slots_;
+  size_t budget_ = 0;
   int64_t cap_points_ = 0;
+  int64_t memory_waits_ = 0;
+  int64_t waiting_id_ = 0;
   std::mutex mu_;
   std::condition_variable cv_, done_cv_;
   std::deque<Request*> queue_;

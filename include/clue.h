@@ -153,11 +153,14 @@ const char* clue_last_error(void);
  * DEVICE pointers; work runs on cuda_stream (NULL = default stream) and the
  * call synchronises that stream before returning.
  * Scratch is one fixed 14 MB area compiled into the library (a static
- * __device__ array that every GPU using the library holds until the process
- * exits), so n is limited to 262,144 points; larger events get CLUE_EINVAL.
- * The first call on a device looks up the area's address (make it before
- * any stream capture).  All calls share the area: calls that overlap on the
- * GPU race; run them one at a time. */
+ * __device__ array), so n is limited to 262,144 points; larger events get
+ * CLUE_EINVAL.  The CUDA runtime creates that array, and loads the kernels'
+ * code, lazily: on each device, the first call does it.  Make that first
+ * call at start-up, before the framework reserves the device's memory for its
+ * pool, and outside any stream capture: a call with n == 0 (every pointer
+ * may then be NULL) does only this set-up.  The array stays until the
+ * process exits.  All calls share the area: calls that overlap on the GPU
+ * race; run them one at a time. */
 int clue_run_event_noalloc(const clue_params* params, int32_t n, const float* x, const float* y,
                            const int32_t* layer, const float* weight, const clue_outputs* out, void* cuda_stream);
 
@@ -287,7 +290,9 @@ typedef struct clue_server_stats {
   double p99_ms;
   double mean_batch_events;
   double max_inflight_seen;
-  int64_t slot_capacity_points; /* largest event (points) one in-flight batch admits */
+  int64_t slot_capacity_points; /* largest event (points) admitted: it fits the budget while the other
+                                   slots hold only their start-up buffers */
+  int64_t memory_waits;         /* times the head of the queue waited for device memory to free up */
 } clue_server_stats;
 
 int clue_server_create(const clue_params* params, const clue_server_config* cfg, clue_server** out);
@@ -295,8 +300,12 @@ int clue_server_destroy(clue_server* s);
 
 /* Queues one event (host pointers).  The inputs are copied before the call
  * returns; the output buffers must stay valid until the request completes.
- * Returns CLUE_ENOMEM when the event alone exceeds one in-flight batch's
- * share of the budget. */
+ * Device memory is shared by the in-flight batches: each slot keeps buffers
+ * for ordinary batches (sized at start within half of an equal share), and an
+ * event larger than those takes, alone, what the others leave of the budget,
+ * waiting for in-flight batches to finish when they hold it.  Returns
+ * CLUE_ENOMEM only when the event could not fit even with every other slot
+ * at its start-up buffers (slot_capacity_points). */
 int clue_server_submit(clue_server* s, int32_t n, const float* x, const float* y, const int32_t* layer,
                        const float* weight, const clue_outputs* out, int64_t* request_id);
 

@@ -1,10 +1,11 @@
 """ctypes front end of the oracle (test infrastructure, not product code).
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
-use this package, as the checker.  ``clue2d``/``clue3d`` run the CPU
-restatement (oracle/clue_oracle.c); ``ref_clue2d``/``ref_clue3d`` run the
-unmodified reference serial code when oracle/_ref was built (reference tree
-present).
+use this package, as the checker (and bench.py to time the CPU baseline).
+``clue2d``/``clue3d`` run the CPU restatement (oracle/clue_oracle.c);
+``ref_clue2d``/``ref_clue2d_batch``/``ref_clue3d`` run the unmodified
+reference serial code when oracle/_ref was built (from the reference tree or
+its install under baseline/_ref).
 """
 import ctypes
 import os
@@ -69,6 +70,11 @@ def lib():
                                                                      _f32p, _f32p, _i32p, _i32p, _i32p, _i32p,
                                                                      _i32p]
         l.oracle_clue3d.restype = ctypes.c_int
+        l.oracle_clue3d_batch.argtypes = ([ctypes.c_int32, _i64p] + [_f32p] * 5 + [_i32p, _f32p, _i32p,
+                                                                                   ctypes.POINTER(Clue3DParams)]
+                                          + [_f32p, _f32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p,
+                                             ctypes.c_int32])
+        l.oracle_clue3d_batch.restype = ctypes.c_int
         _lib = l
     return _lib
 
@@ -88,6 +94,10 @@ def ref_lib():
         l.ref_clue2d.argtypes = [ctypes.c_int32, _f32p, _f32p, _i32p, _f32p, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, _f32p, _f32p, _i32p, _i32p, _i32p]
         l.ref_clue2d.restype = ctypes.c_int
+        l.ref_clue2d_batch.argtypes = [ctypes.c_int32, _i64p, _f32p, _f32p, _i32p, _f32p, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, _f32p, _f32p, _i32p, _i32p, _i32p,
+                                       ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+        l.ref_clue2d_batch.restype = ctypes.c_int
         l.ref_clue3d.argtypes = ([ctypes.c_int32] + [_f32p] * 5 + [_i32p, _f32p, _i32p]
                                  + [ctypes.c_int32, ctypes.c_float, ctypes.c_float, ctypes.c_int32,
                                     ctypes.c_int32, ctypes.c_int32]
@@ -150,6 +160,21 @@ def ref_clue2d(x, y, layer, weight, dc, rhoc, odf):
     return o
 
 
+def ref_clue2d_batch(offsets, x, y, layer, weight, dc, rhoc, odf, n_threads=1):
+    """A CSR batch through the unmodified reference (CLUEAlgoSerial::makeClusters,
+    one algorithm object per thread).  Returns (outputs dict, seconds spent in
+    the makeClusters calls)."""
+    offsets = _c(offsets, np.int64)
+    x, y, w = _c(x, np.float32), _c(y, np.float32), _c(weight, np.float32)
+    layer = _c(layer, np.int32)
+    o = _out2d(x.size)
+    sec = ctypes.c_double(0.0)
+    ref_lib().ref_clue2d_batch(offsets.size - 1, _p(offsets, _i64p), _p(x, _f32p), _p(y, _f32p),
+                               _p(layer, _i32p), _p(w, _f32p), dc, rhoc, odf, *_args2d(o), n_threads,
+                               ctypes.byref(sec))
+    return o, sec.value
+
+
 def _out3d(n):
     return dict(rho=np.empty(n, np.float32), delta_t=np.empty(n, np.float32), delta_l=np.empty(n, np.int32),
                 nh_layer=np.empty(n, np.int32), nh_idx=np.empty(n, np.int32), isSeed=np.empty(n, np.int32),
@@ -179,6 +204,28 @@ def clue3d(pts, **params):
     if nt < 0:
         raise ValueError(f"oracle_clue3d failed ({nt})")
     return o, nt
+
+
+def clue3d_batch(offsets, pts, n_threads=1, **params):
+    """CSR batch of CLUE3D events (``offsets``) through the CPU restatement
+    over ``n_threads`` host threads.  Returns (outputs dict, per-event
+    trackster counts)."""
+    offsets = _c(offsets, np.int64)
+    f, i = _in3d(pts)
+    n = f["z"].size
+    prm = Clue3DParams(**{**REFERENCE_3D_DEFAULTS, **params})
+    o = _out3d(n)
+    nts = np.zeros(offsets.size - 1, np.int32)
+    rc = lib().oracle_clue3d_batch(offsets.size - 1, _p(offsets, _i64p), _p(f["z"], _f32p), _p(f["eta"], _f32p),
+                                   _p(f["phi"], _f32p), _p(f["r_over_absz"], _f32p), _p(f["radius"], _f32p),
+                                   _p(i["layer"], _i32p), _p(f["energy"], _f32p), _p(i["isSilicon"], _i32p),
+                                   ctypes.byref(prm), _p(o["rho"], _f32p), _p(o["delta_t"], _f32p),
+                                   _p(o["delta_l"], _i32p), _p(o["nh_layer"], _i32p), _p(o["nh_idx"], _i32p),
+                                   _p(o["isSeed"], _i32p), _p(o["tracksterIndex"], _i32p), _p(nts, _i32p),
+                                   n_threads)
+    if rc:
+        raise ValueError(f"oracle_clue3d_batch failed ({rc})")
+    return o, nts
 
 
 def ref_clue3d(pts, **params):

@@ -587,3 +587,77 @@ int oracle_clue3d(int32_t n, const float *z, const float *eta, const float *phi,
   o3_free(&w);
   return nt;
 }
+
+/* CSR batch of CLUE3D events over n_threads host threads: event e is
+ * [offsets[e], offsets[e+1]) of every array; n_tracksters[e] receives the
+ * event's trackster count.  Returns 0, or the first event's error code. */
+typedef struct {
+  int32_t n_events;
+  const int64_t *off;
+  const float *z, *eta, *phi, *roa, *radius, *energy;
+  const int32_t *layer, *sil;
+  const oracle3d_params *p;
+  float *rho, *delta_t;
+  int32_t *delta_l, *nh_layer, *nh_idx, *seed, *ti, *nt;
+  int32_t next;
+  int32_t rc;
+  pthread_mutex_t mu;
+} o3_batch;
+
+static void *o3_batch_worker(void *arg) {
+  o3_batch *b = (o3_batch *)arg;
+  for (;;) {
+    pthread_mutex_lock(&b->mu);
+    int32_t e = b->next++;
+    pthread_mutex_unlock(&b->mu);
+    if (e >= b->n_events) break;
+    int64_t s = b->off[e];
+    int32_t n = (int32_t)(b->off[e + 1] - s);
+    int32_t nt = oracle_clue3d(n, b->z + s, b->eta + s, b->phi + s, b->roa + s, b->radius + s, b->layer + s,
+                               b->energy + s, b->sil + s, b->p, b->rho + s, b->delta_t + s, b->delta_l + s,
+                               b->nh_layer + s, b->nh_idx + s, b->seed + s, b->ti + s);
+    b->nt[e] = nt;
+    if (nt < 0) {
+      pthread_mutex_lock(&b->mu);
+      if (!b->rc) b->rc = nt;
+      pthread_mutex_unlock(&b->mu);
+    }
+  }
+  return NULL;
+}
+
+int oracle_clue3d_batch(int32_t n_events, const int64_t *offsets, const float *z, const float *eta,
+                        const float *phi, const float *r_over_absz, const float *radius, const int32_t *layer,
+                        const float *energy, const int32_t *isSilicon, const oracle3d_params *p, float *rho,
+                        float *delta_t, int32_t *delta_l, int32_t *nh_layer, int32_t *nh_idx, int32_t *isSeed,
+                        int32_t *tracksterIndex, int32_t *n_tracksters, int32_t n_threads) {
+  o3_batch b;
+  memset(&b, 0, sizeof(b));
+  b.n_events = n_events;
+  b.off = offsets;
+  b.z = z;
+  b.eta = eta;
+  b.phi = phi;
+  b.roa = r_over_absz;
+  b.radius = radius;
+  b.energy = energy;
+  b.layer = layer;
+  b.sil = isSilicon;
+  b.p = p;
+  b.rho = rho;
+  b.delta_t = delta_t;
+  b.delta_l = delta_l;
+  b.nh_layer = nh_layer;
+  b.nh_idx = nh_idx;
+  b.seed = isSeed;
+  b.ti = tracksterIndex;
+  b.nt = n_tracksters;
+  pthread_mutex_init(&b.mu, NULL);
+  if (n_threads < 1) n_threads = 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)n_threads);
+  for (int t = 0; t < n_threads; ++t) pthread_create(&th[t], NULL, o3_batch_worker, &b);
+  for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+  free(th);
+  pthread_mutex_destroy(&b.mu);
+  return b.rc;
+}

@@ -10,8 +10,12 @@
 // and by tests/golden/make_golden.py (to write the golden vectors).  Build
 // flags: -std=c++17 -O2 -ffp-contract=off, without the reference Makefile's
 // -mavx/-march=native (x86-only, and FMA contraction changes delta bits).
+#include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <cstring>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "plugin-CLUEClusterizer/CLUEAlgoSerial.cc"
@@ -38,6 +42,57 @@ int ref_clue2d(int32_t n, const float* x, const float* y, const int32_t* layer, 
     nearestHigher[i] = out.nearestHigher[i];
     isSeed[i] = out.isSeed[i];
     clusterIndex[i] = out.clusterIndex[i];
+  }
+  return 0;
+}
+
+// CLUEAlgoSerial::makeClusters over a CSR batch of events (event e is
+// [offsets[e], offsets[e+1]) of every array) on n_threads host threads, one
+// CLUEAlgoSerial per thread reused for all of its events, as the reference
+// runs one producer, hence one algorithm object, per EDM stream
+// (src/serial/bin/StreamSchedule.cc:15-39, CLUESerialClusterizer.cc:29-36).
+// Each event's PointsCloud is built before the clock starts and its outputs
+// are copied out after it stops, so *seconds is the wall time of the
+// makeClusters calls alone (their own setup copy and tile clearing included).
+// Events are handed out in order from a shared counter.  Returns 0.
+int ref_clue2d_batch(int32_t n_events, const int64_t* offsets, const float* x, const float* y,
+                     const int32_t* layer, const float* weight, float dc, float rhoc, float odf, float* rho,
+                     float* delta, int32_t* nearestHigher, int32_t* isSeed, int32_t* clusterIndex,
+                     int32_t n_threads, double* seconds) {
+  std::vector<PointsCloud> in(n_events);
+  std::vector<PointsCloudSerial> out(n_events);
+  for (int32_t e = 0; e < n_events; ++e) {
+    const int64_t s = offsets[e], t = offsets[e + 1];
+    in[e].x.assign(x + s, x + t);
+    in[e].y.assign(y + s, y + t);
+    in[e].layer.assign(layer + s, layer + t);
+    in[e].weight.assign(weight + s, weight + t);
+  }
+  if (n_threads < 1) n_threads = 1;
+  // the algorithm objects (each 100 x 10,000 tiles) exist before the clock starts
+  std::vector<std::unique_ptr<CLUEAlgoSerial>> algos;
+  for (int32_t t = 0; t < n_threads; ++t) algos.emplace_back(new CLUEAlgoSerial);
+  std::atomic<int32_t> next{0};
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> th;
+  for (int32_t t = 0; t < n_threads; ++t) {
+    th.emplace_back([&, t]() {
+      for (int32_t e; (e = next.fetch_add(1)) < n_events;) algos[t]->makeClusters(in[e], out[e], dc, rhoc, odf);
+    });
+  }
+  for (auto& t : th) t.join();
+  const auto t1 = std::chrono::steady_clock::now();
+  *seconds = std::chrono::duration<double>(t1 - t0).count();
+  for (int32_t e = 0; e < n_events; ++e) {
+    const int64_t s = offsets[e];
+    const size_t n = out[e].rho.size();
+    for (size_t i = 0; i < n; ++i) {
+      rho[s + i] = out[e].rho[i];
+      delta[s + i] = out[e].delta[i];
+      nearestHigher[s + i] = out[e].nearestHigher[i];
+      isSeed[s + i] = out[e].isSeed[i];
+      clusterIndex[s + i] = out[e].clusterIndex[i];
+    }
   }
   return 0;
 }

@@ -49,7 +49,14 @@ def test_null_arguments_are_einval(cuda_lib):
     assert cuda_lib.clue_server_submit_many(None, 0, None, None, None, None, None, None, None) == C.CLUE_EINVAL
     assert cuda_lib.clue_server_poll(None, 0, 0, None) == C.CLUE_EINVAL
     assert cuda_lib.clue3d_run_batch(None, None, 0, None, None, None, None, 0) == C.CLUE_EINVAL
-    assert cuda_lib.clue_run_event_noalloc(None, 0, None, None, None, None, None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_run_event_noalloc(None, 1, None, None, None, None, None, None) == C.CLUE_EINVAL
+    assert cuda_lib.clue_run_event_noalloc(None, -1, None, None, None, None, None, None) == C.CLUE_EINVAL
+
+
+def test_noalloc_warm_up_without_gpu_reports_cuda_error(cuda_lib):
+    """The n = 0 warm-up call needs a device for its set-up; here there is none."""
+    assert cuda_lib.clue_run_event_noalloc(None, 0, None, None, None, None, None, None) == C.CLUE_ECUDA
+    assert C.last_error()
 
 
 def test_required_bytes_grows_with_points(cuda_lib):

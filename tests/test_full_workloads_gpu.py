@@ -1,0 +1,150 @@
+"""Every event of the benchmarked workloads, bit for bit against the oracle.
+
+The bench line's "bit-exact" rests on these:
+
+* the 4096-event uneven batch (216M points, sizes log-uniform 5k-200k): device
+  resident with the autotuned decomposition (the timed ``value``), and through
+  ``clue_run_batch`` from pinned host memory (the timed ``e2e``: overlapped
+  sub-batches over two device slots);
+* the 1,000 HGCAL-occupancy events (about 325k points each), batched and plain
+  (one event per launch sequence);
+* the 1,000-event CLUE3D batch (2k-20k layer clusters, 100 layers, +-2 sibling
+  layers, criticalDensity 0.5), trackster counts included;
+* CLUE3D on the layer clusters the device bridge builds from the 2D output of
+  the 1,000 HGCAL events, against the oracle run on the bridge's output.
+
+The oracle runs on all host threads (a few seconds per workload).  Reference
+semantics: src/serial/plugin-CLUEClusterizer/CLUEAlgoKernels.h:18-153 and
+src/serial/plugin-CLUETracksterizer/CLUE3DAlgoKernels.h:19-580."""
+import os
+
+import numpy as np
+import pytest
+
+import clue_gb300 as C
+import oracle
+from clue_gb300 import synthetic as S
+
+from _util import KEYS_2D, KEYS_3D, assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+PRM = (1.3, 2.0, 2.0)
+THREADS = os.cpu_count() or 1
+CONFIG4 = dict(n_layers=100, density_sibling_layers=2, nh_sibling_layers=2, critical_density=0.5)
+GPU2ORACLE = dict(rho="rho", delta_transverse="delta_t", delta_layers="delta_l", nh_layer="nh_layer",
+                  nh_index="nh_idx", isSeed="isSeed", tracksterIndex="tracksterIndex")
+
+
+def _dev(torch, b):
+    return {k: torch.from_numpy(np.ascontiguousarray(b[k])).cuda() for k in ("x", "y", "layer", "weight")}
+
+
+def _dev_out(torch, n):
+    return {k: torch.empty(n, dtype=torch.float32 if k in ("rho", "delta") else torch.int32, device="cuda")
+            for k in KEYS_2D}
+
+
+def _host(out):
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def _oracle2d(b):
+    return oracle.clue2d_batch(b["offsets"], b["x"], b["y"], b["layer"], b["weight"], *PRM, n_threads=THREADS)
+
+
+@pytest.fixture(scope="module")
+def uneven():
+    b = S.uneven_batch(4096)
+    return b, _oracle2d(b)
+
+
+@pytest.fixture(scope="module")
+def hgcal():
+    b = S.hgcal_batch(1000, seed=1000)
+    return b, _oracle2d(b)
+
+
+def test_uneven_4096_device_resident_every_event(uneven, cuda_lib):
+    import torch
+    b, want = uneven
+    n = int(b["offsets"][-1])
+    assert n == 216_328_585
+    algo = C.Clusterizer(*PRM, budget_bytes=96 << 30)
+    d, out = _dev(torch, b), _dev_out(torch, n)
+    # the decomposition the bench times (every candidate is digest-checked by the autotuner)
+    algo.autotune(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out)
+    for rep in range(3):  # direct launches, capture, graph replay
+        for v in out.values():
+            v.fill_(-7)
+        algo.run_batch(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY)
+        algo.synchronize()
+        assert_bitexact(_host(out), want, KEYS_2D, label=f"4096 events, device resident, run {rep}")
+    algo.close()
+
+
+def test_uneven_4096_pinned_host_memory_every_event(uneven, cuda_lib):
+    import torch
+    b, want = uneven
+    n = int(b["offsets"][-1])
+    algo = C.Clusterizer(*PRM, budget_bytes=96 << 30)
+    hin = {k: torch.from_numpy(np.ascontiguousarray(b[k])).pin_memory() for k in ("x", "y", "layer", "weight")}
+    hout = {k: torch.full((n,), -7, dtype=torch.float32 if k in ("rho", "delta") else torch.int32).pin_memory()
+            for k in KEYS_2D}
+    algo.run_batch(b["offsets"], hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
+    st = algo.last_run_stats()
+    assert st["h2d_bytes"] >= 16 * n and st["d2h_bytes"] >= 20 * n
+    assert_bitexact({k: v.numpy() for k, v in hout.items()}, want, KEYS_2D, label="4096 events, pinned host")
+    algo.close()
+
+
+def test_hgcal_1000_batched_and_plain_every_event(hgcal, cuda_lib):
+    import torch
+    b, want = hgcal
+    n = int(b["offsets"][-1])
+    algo = C.Clusterizer(*PRM, budget_bytes=96 << 30)
+    d, out = _dev(torch, b), _dev_out(torch, n)
+    algo.autotune(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out)
+    for flags, label in ((0, "batched"), (C.PLAIN, "plain")):
+        for v in out.values():
+            v.fill_(-7)
+        algo.run_batch(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
+        algo.synchronize()
+        assert_bitexact(_host(out), want, KEYS_2D, label=f"1,000 HGCAL events, {label}")
+    algo.close()
+
+
+def test_clue3d_1000_events_every_event():
+    b3 = S.clue3d_batch(1000, seed0=1000, n_layers=100)
+    algo = C.Clusterizer(*PRM, budget_bytes=32 << 30)
+    got, nts = algo.run_clue3d(b3["offsets"], b3, params=CONFIG4)
+    algo.close()
+    want, wnt = oracle.clue3d_batch(b3["offsets"], b3, n_threads=THREADS, **CONFIG4)
+    assert np.array_equal(nts, wnt)
+    assert_bitexact({GPU2ORACLE[k]: v for k, v in got.items()}, want, KEYS_3D, label="1,000 CLUE3D events")
+
+
+def test_clue3d_on_the_bridge_output_of_hgcal_1000(hgcal, cuda_lib):
+    """The chain the bench's clue3d_from_config2 leg times: 2D on the device,
+    the bridge on the device, CLUE3D on its output; the CLUE3D outputs against
+    the oracle on the same (GPU-built) layer clusters, every event."""
+    import torch
+    b, want2d = hgcal
+    n = int(b["offsets"][-1])
+    algo = C.Clusterizer(*PRM, budget_bytes=96 << 30)
+    d, out = _dev(torch, b), _dev_out(torch, n)
+    algo.run_batch(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY)
+    algo.synchronize()
+    coff, lc = algo.layer_clusters(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out)
+    assert int(coff[-1]) == int(np.count_nonzero(want2d["isSeed"]))
+    n3 = int(coff[-1])
+    out3 = {k: torch.empty(n3, dtype=torch.float32 if k in ("rho", "delta_transverse") else torch.int32,
+                           device="cuda") for k in GPU2ORACLE}
+    _, nts = algo.run_clue3d(coff, lc, params=CONFIG4, flags=C.DEVICE_MEMORY, out=out3)
+    algo.synchronize()
+    clusters = {k: v.cpu().numpy() for k, v in lc.items()}
+    got = {GPU2ORACLE[k]: v.cpu().numpy() for k, v in out3.items()}
+    algo.close()
+    want, wnt = oracle.clue3d_batch(coff, clusters, n_threads=THREADS, **CONFIG4)
+    assert_bitexact(got, want, KEYS_3D, label="CLUE3D on the bridge output of 1,000 HGCAL events")
+    assert wnt.sum() > 0

@@ -97,7 +97,9 @@ def _uniform_event(n, seed):
                 layer=rng.integers(0, 100, n).astype(np.int32), weight=rng.exponential(1.0, n).astype(np.float32))
 
 
-def test_admission_rejects_an_event_larger_than_a_slot():
+def test_admission_rejects_an_event_larger_than_the_budget_admits():
+    """slot_capacity_points is the largest event that fits the budget while
+    the other slot holds its start-up buffers; one point more is refused."""
     srv = C.Server(*PRM, budget_bytes=96 << 20, max_inflight=2, max_batch_events=4)
     cap = srv.stats()["slot_capacity_points"]
     assert cap > 1000
@@ -108,4 +110,30 @@ def test_admission_rejects_an_event_larger_than_a_slot():
     rid, out = srv.submit(**small)  # half a slot still fits
     assert srv.poll(rid, timeout_ms=60000)[0] == C.CLUE_OK
     assert_bitexact(out, oracle.clue2d(small["x"], small["y"], small["layer"], small["weight"], *PRM))
+    srv.close()
+
+
+def test_large_events_share_the_budget_and_wait_for_memory():
+    """Two events each larger than half the budget's share: the first takes
+    what the idle slot leaves of the budget, the second waits at the head of
+    the queue until the first batch has finished (its slot then gives its
+    memory back), instead of being refused.  Both results are bit-identical
+    to the oracle, as is a small event queued behind them."""
+    budget = 96 << 20
+    srv = C.Server(*PRM, budget_bytes=budget, max_inflight=2, max_batch_events=4)
+    cap = srv.stats()["slot_capacity_points"]
+    # each above what an equal split of the budget would admit, and two of
+    # them together above the budget (memory_waits below shows the wait)
+    big = int(cap * 0.7)
+    evs = [_uniform_event(big, 11), _uniform_event(big, 12), _uniform_event(5000, 13)]
+    off = np.array([0, big, 2 * big, 2 * big + 5000], np.int64)
+    cat = {k: np.concatenate([e[k] for e in evs]) for k in ("x", "y", "layer", "weight")}
+    reqs = srv.submit_many(off, cat["x"], cat["y"], cat["layer"], cat["weight"])
+    srv.drain(timeout_ms=120000)
+    for (rid, out), e in zip(reqs, evs):
+        assert srv.poll(rid, timeout_ms=0)[0] == C.CLUE_OK
+        assert_bitexact(out, oracle.clue2d(e["x"], e["y"], e["layer"], e["weight"], *PRM))
+    st = srv.stats()
+    assert st["memory_waits"] >= 1, st
+    assert st["completed"] == 3
     srv.close()
