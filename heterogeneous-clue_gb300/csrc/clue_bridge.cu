@@ -42,32 +42,127 @@ __device__ __forceinline__ int32_t event_of(const int64_t* __restrict__ off, int
   return lo;
 }
 
-__global__ void k_bridge_count(int32_t E, int64_t N, const int64_t* __restrict__ off,
-                               const int32_t* __restrict__ seed, int32_t* __restrict__ counts) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-    if (seed[i]) atomicAdd(&counts[event_of(off, E, i)], 1);
+// Points per block of the point kernels: each block finds the event of its
+// first point once and then follows event boundaries forwards.
+constexpr int kBridgeChunk = 4096;
+constexpr int kBridgeThreads = 256;
+
+int chunks_for(int64_t n) { return (int)((n + kBridgeChunk - 1) / kBridgeChunk); }
+
+// Fixed-point weight, round(w * 2^24) as the double formula gives it: the
+// float product is exact (a power-of-two scale) below 2^100, and converts with
+// the same rounding; NaN, infinities and huge weights take the double formula.
+__device__ __forceinline__ unsigned long long fx_weight(float w) {
+  if (fabsf(w) < 1.2676506e30f) return (unsigned long long)__float2ll_rn(w * 16777216.f);
+  return (unsigned long long)__double2ll_rn((double)w * kWScale);
 }
 
-__global__ void k_bridge_accumulate(int32_t E, int64_t N, const int64_t* __restrict__ off,
-                                    const int64_t* __restrict__ coff, const float* __restrict__ x,
-                                    const float* __restrict__ y, const float* __restrict__ w,
-                                    const int32_t* __restrict__ seed, const int32_t* __restrict__ ci,
-                                    unsigned long long* __restrict__ acc, int32_t* __restrict__ seed_of,
-                                    int32_t* __restrict__ flags) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t c = ci[i];
-    if (c < 0) continue;
-    const int32_t e = event_of(off, E, i);
-    if (c >= coff[e + 1] - coff[e]) {
-      atomicExch(&flags[kFlagError], 1);
-      continue;
+// Fixed-point weighted coordinate, round(w * v * 2^16) to nearest even, as
+// the double formula gives it (the double product of two floats is exact):
+// computed on the integer significands (a 48-bit product, shifted with
+// round-half-even), without FP64, which is slow on this GPU.  Infinities,
+// NaN and products that may not fit 63 bits take the double formula.
+__device__ __forceinline__ unsigned long long fx_pos(float w, float v) {
+  const unsigned uw = __float_as_uint(w), uv = __float_as_uint(v);
+  int ew = (uw >> 23) & 0xff, ev = (uv >> 23) & 0xff;
+  unsigned long long mw = uw & 0x7fffffu, mv = uv & 0x7fffffu;
+  if (ew == 0xff || ev == 0xff) return (unsigned long long)__double2ll_rn((double)w * (double)v * kPScale);
+  if (ew) mw |= 0x800000u; else ew = 1;
+  if (ev) mv |= 0x800000u; else ev = 1;
+  const unsigned long long m = mw * mv;          // below 2^48
+  const int sh = (ew - 150) + (ev - 150) + 16;   // value = m * 2^sh
+  if (sh > 14) return (unsigned long long)__double2ll_rn((double)w * (double)v * kPScale);
+  unsigned long long q;
+  if (sh >= 0) {
+    q = m << sh;
+  } else if (-sh > 49) {
+    q = 0;  // below one half
+  } else {
+    const int sr = -sh;
+    q = m >> sr;
+    const unsigned long long rem = m & ((1ull << sr) - 1), half = 1ull << (sr - 1);
+    if (rem > half || (rem == half && (q & 1))) ++q;
+  }
+  return ((uw ^ uv) >> 31) ? (0ull - q) : q;
+}
+
+__global__ void __launch_bounds__(kBridgeThreads) k_bridge_count(int32_t E, int64_t N,
+                                                                   const int64_t* __restrict__ off,
+                                                                   const int32_t* __restrict__ seed,
+                                                                   int32_t* __restrict__ counts) {
+  __shared__ int32_t s_e;
+  const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
+  if (threadIdx.x == 0) s_e = event_of(off, E, c0);
+  __syncthreads();
+  int32_t e = s_e;
+  for (int k = 0; k < kBridgeChunk / kBridgeThreads; ++k) {
+    const int64_t i = c0 + (int64_t)k * kBridgeThreads + threadIdx.x;
+    int32_t key = -1;
+    if (i < N) {
+      while (off[e + 1] <= i) ++e;  // i grows with k
+      if (seed[i]) key = e;
     }
-    const int64_t g = coff[e] + c;
-    const double wd = (double)w[i];
-    atomicAdd(&acc[3 * g], (unsigned long long)__double2ll_rn(wd * kWScale));
-    atomicAdd(&acc[3 * g + 1], (unsigned long long)__double2ll_rn(wd * (double)x[i] * kPScale));
-    atomicAdd(&acc[3 * g + 2], (unsigned long long)__double2ll_rn(wd * (double)y[i] * kPScale));
-    if (seed[i]) seed_of[g] = (int32_t)i;
+    // one increment per event among the warp's seeds
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[key], __popc(grp));
+  }
+}
+
+// The sums of a cluster are exact integers, so they may be added in any
+// grouping: lanes holding the same cluster in a run of consecutive lanes (the
+// usual case: a cluster's points are mostly consecutive) add theirs first and
+// the run's last lane makes the three atomic additions.
+__global__ void __launch_bounds__(kBridgeThreads) k_bridge_accumulate(
+    int32_t E, int64_t N, const int64_t* __restrict__ off, const int64_t* __restrict__ coff,
+    const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ w,
+    const int32_t* __restrict__ seed, const int32_t* __restrict__ ci, unsigned long long* __restrict__ acc,
+    int32_t* __restrict__ seed_of, int32_t* __restrict__ flags) {
+  __shared__ int32_t s_e;
+  const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
+  if (threadIdx.x == 0) s_e = event_of(off, E, c0);
+  __syncthreads();
+  int32_t e = s_e;
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < kBridgeChunk / kBridgeThreads; ++k) {
+    const int64_t i = c0 + (int64_t)k * kBridgeThreads + threadIdx.x;
+    int32_t g = -1;
+    unsigned long long v0 = 0, v1 = 0, v2 = 0;
+    if (i < N) {
+      while (off[e + 1] <= i) ++e;  // i grows with k
+      const int32_t c = ci[i];
+      if (c >= 0) {
+        if (c >= coff[e + 1] - coff[e]) {
+          atomicExch(&flags[kFlagError], 1);
+        } else {
+          g = (int32_t)(coff[e] + c);
+          const float wi = w[i];
+          v0 = fx_weight(wi);
+          v1 = fx_pos(wi, x[i]);
+          v2 = fx_pos(wi, y[i]);
+          if (seed[i]) seed_of[g] = (int32_t)i;
+        }
+      }
+    }
+    const int32_t gp = __shfl_up_sync(0xffffffffu, g, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || gp != g);
+    const int first = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // the run's first lane
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t0 = __shfl_up_sync(0xffffffffu, v0, o);
+      const unsigned long long t1 = __shfl_up_sync(0xffffffffu, v1, o);
+      const unsigned long long t2 = __shfl_up_sync(0xffffffffu, v2, o);
+      if (lane - o >= first) {
+        v0 += t0;
+        v1 += t1;
+        v2 += t2;
+      }
+    }
+    const int32_t gn = __shfl_down_sync(0xffffffffu, g, 1);
+    if (g >= 0 && (lane == 31 || gn != g)) {
+      atomicAdd(&acc[3 * (int64_t)g], v0);
+      atomicAdd(&acc[3 * (int64_t)g + 1], v1);
+      atomicAdd(&acc[3 * (int64_t)g + 2], v2);
+    }
   }
 }
 
@@ -164,7 +259,7 @@ int clue_bridge_count(clue_handle* hh, int32_t E, const int64_t* off, const int3
         (e = cudaMemsetAsync(P(clue::B_COUNT), 0, 4 * (size_t)E, s)))
       return cuda_error(e, "bridge set-up");
     if (N > 0)
-      clue::k_bridge_count<<<clue::grid_for(N), 256, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
+      clue::k_bridge_count<<<clue::chunks_for(N), clue::kBridgeThreads, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
                                                               isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
     if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_count");
     std::vector<int32_t> counts(E);
@@ -228,7 +323,7 @@ int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, c
     auto* acc = static_cast<unsigned long long*>(P(clue::B_ACC));
     auto* seed_of = static_cast<int32_t*>(P(clue::B_SEED));
     if (N > 0)
-      clue::k_bridge_accumulate<<<clue::grid_for(N), 256, 0, s>>>(
+      clue::k_bridge_accumulate<<<clue::chunks_for(N), clue::kBridgeThreads, 0, s>>>(
           E, N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int64_t*>(P(clue::B_COFF)), x, y,
           weight, isSeed, clusterIndex, acc, seed_of, flags);
     if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_accumulate");

@@ -1,4 +1,4 @@
-// Resident host-copy pool of the serving path (host-only C++, no CUDA).
+// Resident host-copy pool (host-only C++, no CUDA).
 #pragma once
 
 #include <algorithm>
@@ -13,12 +13,14 @@
 
 namespace clue {
 
-// Host copies of the serving path (request staging and result delivery).
-// Sets of 512 KB or more are cut into 256 KB pieces shared by the calling
-// thread and resident helper threads (no thread is started per copy).
-// Several callers (submitting clients, the scheduler) may run sets at once:
-// a helper takes at most four pieces of a set before it moves on to the next
-// set, so that no set waits behind a large one.
+// Host copies of the serving path (request staging and result delivery) and
+// the host passes of the pipelined host-memory path.  Work is cut into
+// pieces shared by the calling thread and resident helper threads (no thread
+// is started per call): copy sets of 512 KB or more in 256 KB pieces, or a
+// caller's own function over numbered pieces (for_pieces).  Several callers
+// (submitting clients, the scheduler) may run sets at once: a helper takes at
+// most four pieces of a set before it moves on to the next set, so that no
+// set waits behind a large one.
 struct CopyTask {
   void* dst;
   const void* src;
@@ -34,10 +36,11 @@ class CopyPool {
       try {
         threads_.emplace_back([this] { loop(); });
       } catch (...) {
-        break;  // fewer helpers: callers copy their own pieces
+        break;  // fewer helpers: callers do their own pieces
       }
     }
   }
+  bool started() const { return !threads_.empty(); }
 
   void stop() {
     {
@@ -58,12 +61,28 @@ class CopyPool {
         if (t.bytes) memcpy(t.dst, t.src, t.bytes);
       return;
     }
-    Job job;
+    std::vector<CopyTask> pieces;
     for (const auto& t : tasks)
       for (size_t o = 0; o < t.bytes; o += kPiece)
-        job.pieces.push_back({static_cast<char*>(t.dst) + o, static_cast<const char*>(t.src) + o,
-                              std::min(kPiece, t.bytes - o)});
-    job.left = job.pieces.size();
+        pieces.push_back({static_cast<char*>(t.dst) + o, static_cast<const char*>(t.src) + o,
+                          std::min(kPiece, t.bytes - o)});
+    for_pieces(pieces.size(), [&](size_t i) { memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes); });
+  }
+
+  // Calls f(0) .. f(n - 1), each once, on the calling thread and the helpers;
+  // returns when all calls have returned.
+  template <class F>
+  void for_pieces(size_t n, F&& f) {
+    if (n == 0) return;
+    if (threads_.empty() || n == 1) {
+      for (size_t i = 0; i < n; ++i) f(i);
+      return;
+    }
+    Job job;
+    job.n = n;
+    job.fn = [](void* ctx, size_t i) { (*static_cast<F*>(ctx))(i); };
+    job.ctx = &f;
+    job.left = n;
     {
       std::lock_guard<std::mutex> g(mu_);
       jobs_.push_back(&job);
@@ -79,15 +98,17 @@ class CopyPool {
 
  private:
   struct Job {
-    std::vector<CopyTask> pieces;
+    size_t n = 0;
+    void (*fn)(void*, size_t) = nullptr;
+    void* ctx = nullptr;
     std::atomic<size_t> next{0};
     std::atomic<size_t> left{0};
     int holders = 0;  // helpers working on it (guarded by mu_)
   };
 
   static void work(Job& j, size_t max_pieces = SIZE_MAX) {
-    for (size_t i, k = 0; k < max_pieces && (i = j.next.fetch_add(1)) < j.pieces.size(); ++k) {
-      memcpy(j.pieces[i].dst, j.pieces[i].src, j.pieces[i].bytes);
+    for (size_t i, k = 0; k < max_pieces && (i = j.next.fetch_add(1)) < j.n; ++k) {
+      j.fn(j.ctx, i);
       j.left.fetch_sub(1);
     }
   }
@@ -99,7 +120,7 @@ class CopyPool {
       if (stop_) return;
       Job* j = jobs_.front();
       jobs_.pop_front();
-      if (j->next.load() >= j->pieces.size()) {  // nothing left to take: let the owner finish it
+      if (j->next.load() >= j->n) {  // nothing left to take: let the owner finish it
         done_cv_.notify_all();
         continue;
       }

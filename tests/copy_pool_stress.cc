@@ -1,7 +1,9 @@
-// Stress test of the serving path's host-copy pool: several threads run copy
-// sets of random sizes (below and above the parallel threshold) at once;
-// every byte must arrive and every run must return.
+// Stress test of the resident host-copy pool: several threads run copy sets
+// of random sizes (below and above the parallel threshold) and functions over
+// numbered pieces at once; every byte must arrive, every piece must run
+// exactly once, and every run must return.
 #include <cstdio>
+#include <atomic>
 #include <cstdlib>
 #include <random>
 #include <thread>
@@ -31,6 +33,13 @@ int main(int argc, char** argv) {
       pool.run(tasks);
       for (int k = 0; k < nt; ++k)
         if (src[k] != dst[k]) bad++;
+      // a function over numbered pieces: every piece runs exactly once
+      const size_t np = rng() % 300;
+      std::vector<std::atomic<int>> hits(np);
+      for (auto& hh : hits) hh = 0;
+      pool.for_pieces(np, [&](size_t i) { hits[i].fetch_add(1); });
+      for (auto& hh : hits)
+        if (hh.load() != 1) bad++;
     }
   };
   std::vector<std::thread> th;

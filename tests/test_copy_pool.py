@@ -1,6 +1,7 @@
-"""The serving path's host-copy pool (csrc/copy_pool.h) on the CPU: three
-threads run copy sets of random sizes at once through one pool; every byte
-must arrive and every run must return, plain and under ThreadSanitizer."""
+"""The resident host-copy pool (csrc/copy_pool.h) on the CPU: three threads
+run copy sets of random sizes and functions over numbered pieces at once
+through one pool; every byte must arrive, every piece must run once and every
+run must return, plain and under ThreadSanitizer."""
 import os
 import shutil
 import subprocess
