@@ -16,8 +16,9 @@
 //   k3_row_scan   per event: first position of each row
 //   k3_scatter    place clusters into their rows (arbitrary order)
 //   k3_row_sort   order each row by (phi bin, index)
-//   k3_density    KernelCalculateDensitySoA (:26-150)
-//   k3_nh         KernelComputeDistanceToHigherSoA (:286-392)
+//   k3_search<true>   KernelCalculateDensitySoA (:26-150), one block per
+//                     (event, slab of layers) with the slab's rows staged
+//   k3_search<false>  KernelComputeDistanceToHigherSoA (:286-392), likewise
 //   k3_flags      seeds, outliers, parent pointers (:509-560)
 //   k3_finish     per event: trackster ids by seed rank, pointer jumping
 //                 along nearestHigher, labels (:564-577)
@@ -188,9 +189,64 @@ __global__ void k3_row_sort(Batch3D b) {
   if (atomicOr(m + (col >> 6), bit) & bit) atomicOr(m + 1, 1ull << 63);
 }
 
-// Visits the entries of one row whose phi column lies in the window
+// The rows of one event as the searches see them: the whole event in global
+// memory, or a staged copy of a range of rows in shared memory.  Positions
+// are sorted positions (global, or relative to the first staged entry).
+struct RowsGlobal {
+  const unsigned long long* mask;  // 2 words per row of the event
+  const int32_t* rstart;           // first sorted position of each row of the event
+  const float4* cand;
+  const int32_t* scol;
+  __device__ __forceinline__ unsigned long long m0(int r) const { return mask[2 * r]; }
+  __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * r + 1]; }
+  __device__ __forceinline__ int start(int r) const { return rstart[r]; }
+  __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
+  __device__ __forceinline__ int col(int q) const { return scol[q]; }
+};
+
+struct RowsStaged {
+  const unsigned long long* mask;  // 2 words per staged row
+  const int32_t* rstart;           // relative to the first staged entry
+  const float4* cand;
+  const uint8_t* scol;
+  int row_lo;  // first staged row
+  __device__ __forceinline__ unsigned long long m0(int r) const { return mask[2 * (r - row_lo)]; }
+  __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * (r - row_lo) + 1]; }
+  __device__ __forceinline__ int start(int r) const { return rstart[r - row_lo]; }
+  __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
+  __device__ __forceinline__ int col(int q) const { return scol[q]; }
+};
+
+// Visits the entries of rows [s, t) whose phi column lies in the window
 // [p0, p1] (p0 may be negative, p1 may exceed 125), in the reference's
 // order: iphi_it = p0..p1 mapped modulo 126.
+template <class V, class F>
+__device__ __forceinline__ void visit_row(const V& v, int s, int t, int p0, int p1, F&& f) {
+  if (p0 >= 0 && p1 < kPhiBins) {
+    for (int q = s; q < t; ++q) {
+      const int c = v.col(q);
+      if (c > p1) break;
+      if (c >= p0) f(q);
+    }
+    return;
+  }
+  int a0, a1, c0, c1;  // first arc [a0, a1], then [c0, c1]
+  if (p0 < 0) {
+    a0 = p0 + kPhiBins; a1 = kPhiBins - 1; c0 = 0; c1 = p1;
+  } else {
+    a0 = p0; a1 = kPhiBins - 1; c0 = 0; c1 = p1 - kPhiBins;
+  }
+  for (int q = s; q < t; ++q) {
+    const int c = v.col(q);
+    if (c >= a0 && c <= a1) f(q);
+  }
+  for (int q = s; q < t; ++q) {
+    const int c = v.col(q);
+    if (c > c1) break;
+    if (c >= c0) f(q);
+  }
+}
+
 // Entries of a row whose phi column lies in [a, c] (0 <= a <= c <= 125) are
 // one run of the row (entries are sorted by column): its first position and
 // length, from the column-occupancy mask, when no column repeats.
@@ -203,11 +259,11 @@ __device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long l
 
 // visit_row() for row r through its occupancy mask: the row start is read
 // only when the window holds an entry, and the row is not scanned.
-template <class F>
-__device__ __forceinline__ void visit_row_masked(const Batch3D& b, int64_t r, int p0, int p1, F&& f) {
-  const unsigned long long m0 = b.row_mask[2 * r], m1 = b.row_mask[2 * r + 1];
+template <class V, class F>
+__device__ __forceinline__ void visit_row_masked(const V& v, int r, int p0, int p1, F&& f) {
+  const unsigned long long m0 = v.m0(r), m1 = v.m1(r);
   if (m1 >> 63) {  // a column holds several entries: walk the row
-    visit_row(b, b.row_start[r], b.row_start[r + 1], p0, p1, f);
+    visit_row(v, v.start(r), v.start(r + 1), p0, p1, f);
     return;
   }
   int a0, c0, a1 = 0, c1 = -1;  // first run [a0, c0], then [a1, c1] (wrapping windows)
@@ -221,127 +277,161 @@ __device__ __forceinline__ void visit_row_masked(const Batch3D& b, int64_t r, in
   const int lo0 = bits_below(m0, m1, a0), n0 = bits_below(m0, m1, c0 + 1) - lo0;
   const int n1 = c1 >= a1 ? bits_below(m0, m1, c1 + 1) : 0;  // the second run starts at column 0
   if (n0 + n1 == 0) return;
-  const int s = b.row_start[r];
+  const int s = v.start(r);
   for (int q = s + lo0; q < s + lo0 + n0; ++q) f(q);
   for (int q = s; q < s + n1; ++q) f(q);
 }
 
-template <class F>
-__device__ __forceinline__ void visit_row(const Batch3D& b, int s, int t, int p0, int p1, F&& f) {
-  if (p0 >= 0 && p1 < kPhiBins) {
-    for (int q = s; q < t; ++q) {
-      const int c = b.scol[q];
-      if (c > p1) break;
-      if (c >= p0) f(q);
-    }
-    return;
-  }
-  int a0, a1, c0, c1;  // first arc [a0, a1], then [c0, c1]
-  if (p0 < 0) {
-    a0 = p0 + kPhiBins; a1 = kPhiBins - 1; c0 = 0; c1 = p1;
-  } else {
-    a0 = p0; a1 = kPhiBins - 1; c0 = 0; c1 = p1 - kPhiBins;
-  }
-  for (int q = s; q < t; ++q) {
-    const int c = b.scol[q];
-    if (c >= a0 && c <= a1) f(q);
-  }
-  for (int q = s; q < t; ++q) {
-    const int c = b.scol[q];
-    if (c > c1) break;
-    if (c >= c0) f(q);
-  }
-}
-
-// 40 registers (6 blocks per SM): 4.76 ms against 5.26 ms at the compiler's
-// 56 on the 1,000-event batch
-__global__ void __launch_bounds__(256, 6) k3_density(Batch3D b, Params3D P) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= b.n_points) return;
-  const int e = event_of(b.offsets, b.n_events, p);
-  const int64_t es = b.offsets[e];
-  const int i = b.sorted[p];  // clusters processed in tile order for locality
-  const int64_t gi = es + i;
-  const int li = b.layer[gi];
-  if (b.key[gi] < 0) return;
+// One cluster's density (KernelCalculateDensitySoA, :26-150) over the rows
+// in `v`; self is the cluster's own position there.
+template <class V>
+__device__ __forceinline__ float density_of(const V& v, const Params3D& P, int li, int eb, int pb, float phi_i,
+                                            float zi, float r0, float thr, int self) {
   int lo, hi;
   layer_window(li, P.dens_sib, P.n_layers, 0, &lo, &hi);
-  const float eta_i = b.eta[gi], phi_i = b.phi[gi], zi = b.z[gi];
-  const int eb = eta_bin(eta_i, P), pb = phi_bin(phi_i, P);
-  const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
-  const float r0 = __fmul_rn(b.roa[gi], zi);
-  const int64_t rbase = (int64_t)e * b.n_rows;
   float rho = 0.f;
   for (int cl = lo; cl <= hi; ++cl) {
     const bool same = (cl == li);
     const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
     const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
-      const int64_t r = rbase + (int64_t)cl * kEtaBins + ie;
-      visit_row_masked(b, r, pb - 2, pb + 2, [&](int q) {
-        const float4 cj = b.cand[q];  // {roa, phi, energy, -}; q == p is the cluster itself
+      visit_row_masked(v, cl * kEtaBins + ie, pb - 2, pb + 2, [&](int q) {
+        const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
         const float r1 = __fmul_rn(cj.x, zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
         const float d0 = __fsub_rn(r0, r1);
         const float a = __fmul_rn(d0, d0);
         const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
-        if (__fadd_rn(a, c) < thr) rho = __fadd_rn(rho, __fmul_rn((q == p) ? 1.f : coef, cj.z));
+        if (__fadd_rn(a, c) < thr) rho = __fadd_rn(rho, __fmul_rn((q == self) ? 1.f : coef, cj.z));
       });
     }
   }
-  b.rho[gi] = rho;
-  reinterpret_cast<float*>(b.cand)[4 * p + 3] = rho;
+  return rho;
 }
 
-// 40 registers (6 blocks per SM), as k3_density: 4.76 -> 4.58 ms per batch
-__global__ void __launch_bounds__(256, 6) k3_nh(Batch3D b, Params3D P) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= b.n_points) return;
-  const int e = event_of(b.offsets, b.n_events, p);
-  const int64_t es = b.offsets[e];
-  const int i = b.sorted[p];
-  const int64_t gi = es + i;
-  const int li = b.layer[gi];
-  if (b.key[gi] < 0) return;
+// One cluster's nearest higher (KernelComputeDistanceToHigherSoA, :286-392)
+// over the rows in `v`: best squared distance (FLT_MAX: none), its sqrt, the
+// layer distance, the layer and the position in `v`.
+struct Nh3 {
+  float best = FLT_MAX, best_t = FLT_MAX;
+  int best_l = INT_MAX, nl = -1, nq = -1;
+};
+
+template <class V>
+__device__ __forceinline__ Nh3 nearest_higher_of(const V& v, const Params3D& P, int li, int eb, int pb, float phi_i,
+                                                 float zi, float r0, float rho_i) {
   int lo, hi;
   layer_window(li, P.nh_sib, P.n_layers, 1, &lo, &hi);
-  const float eta_i = b.eta[gi], phi_i = b.phi[gi], zi = b.z[gi], rho_i = b.rho[gi];
-  const int eb = eta_bin(eta_i, P), pb = phi_bin(phi_i, P);
-  const float r0 = __fmul_rn(b.roa[gi], zi);
-  const int64_t rbase = (int64_t)e * b.n_rows;
-  float best = FLT_MAX, best_t = FLT_MAX;
-  int best_l = INT_MAX, nl = -1, ni = -1;
+  Nh3 o;
   for (int cl = lo; cl <= hi; ++cl) {
     if (!P.nh_same && cl == li) continue;
     const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
-      const int64_t r = rbase + (int64_t)cl * kEtaBins + ie;
-      visit_row_masked(b, r, pb - 1, pb + 1, [&](int q) {
-        const float4 cj = b.cand[q];  // {roa, phi, energy, rho}
+      visit_row_masked(v, cl * kEtaBins + ie, pb - 1, pb + 1, [&](int q) {
+        const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
         const float r1 = __fmul_rn(cj.x, zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
         const float d0 = __fsub_rn(r0, r1);
         const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
-        if (cj.w > rho_i && d <= best) {  // "<=": the last candidate wins a tie
-          best = d;
-          best_t = __fsqrt_rn(d);
-          best_l = abs(cl - li);
-          nl = cl;
-          ni = b.sorted[q];
+        if (cj.w > rho_i && d <= o.best) {  // "<=": the last candidate wins a tie
+          o.best = d;
+          o.best_t = __fsqrt_rn(d);
+          o.best_l = abs(cl - li);
+          o.nl = cl;
+          o.nq = q;
         }
       });
     }
   }
-  if (best != FLT_MAX) {
-    b.delta_t[gi] = best_t;
-    b.delta_l[gi] = best_l;
-    b.nh_l[gi] = nl;
-    b.nh_i[gi] = ni;
-  } else {
-    b.delta_t[gi] = FLT_MAX;
-    b.delta_l[gi] = INT_MAX;
-    b.nh_l[gi] = -1;
-    b.nh_i[gi] = -1;
+  return o;
+}
+
+// Staging of the searches: one block per (event, slab of kSlabLayers
+// layers).  The block copies the rows of the slab's layers and of the
+// sibling layers around them (occupancy masks, row starts, phi columns and
+// the 16-byte candidate records) into shared memory once, then runs the
+// searches of the slab's clusters from there.  A cluster whose window leaves
+// the staged rows (the phi bin 126 quirk can move a cluster into the next
+// layer's first row) and a slab larger than the staging area read the global
+// arrays instead; either way the visiting order and arithmetic are the
+// reference's.
+constexpr int kSlabLayers = 4;
+constexpr int kSlabThreads = 256;
+constexpr int kSlabMaxRows = 512;
+constexpr int kSlabMaxCand = 2048;
+constexpr size_t kSlabSmem = 16 * (size_t)kSlabMaxRows + 4 * (size_t)(kSlabMaxRows + 1) +
+                             16 * (size_t)kSlabMaxCand + (size_t)kSlabMaxCand;
+
+template <bool kDensity>
+__global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D P, int n_slabs) {
+  __shared__ __align__(16) unsigned char sm3[kSlabSmem];
+  unsigned long long* s_mask = reinterpret_cast<unsigned long long*>(sm3);
+  float4* s_cand = reinterpret_cast<float4*>(sm3 + 16 * (size_t)kSlabMaxRows);
+  int32_t* s_rs = reinterpret_cast<int32_t*>(sm3 + 16 * (size_t)kSlabMaxRows + 16 * (size_t)kSlabMaxCand);
+  uint8_t* s_col = reinterpret_cast<uint8_t*>(s_rs + kSlabMaxRows + 1);
+  const int e = blockIdx.x / n_slabs;
+  const int L0 = (blockIdx.x % n_slabs) * kSlabLayers;
+  const int L1 = min(L0 + kSlabLayers, P.n_layers);
+  const int sib = kDensity ? P.dens_sib : P.nh_sib;
+  const int R = b.n_rows;
+  const int64_t rbase = (int64_t)e * R;
+  const int32_t* rs = b.row_start + rbase;
+  const int q_lo = rs[L0 * kEtaBins], q_hi = rs[L1 * kEtaBins];
+  if (q_lo >= q_hi) return;
+  // rows of layers [L0 - sib, L1 + sib) and the first row after them (the
+  // reference's eta window reaches row 34 of a layer, the next layer's row 0)
+  const int hl0 = max(L0 - max(sib, 0), 0), hl1 = min(L1 + max(sib, 0), P.n_layers);
+  const int row_lo = hl0 * kEtaBins, row_hi = hl1 * kEtaBins;  // inclusive; row_hi <= R - 2
+  const int nrows = row_hi - row_lo + 1;
+  const int pos_lo = rs[row_lo], pos_hi = rs[row_hi + 1];
+  const bool staged = nrows <= kSlabMaxRows && pos_hi - pos_lo <= kSlabMaxCand;
+  if (staged) {
+    const unsigned long long* gm = b.row_mask + 2 * (rbase + row_lo);
+    for (int i = threadIdx.x; i < 2 * nrows; i += kSlabThreads) s_mask[i] = gm[i];
+    for (int i = threadIdx.x; i <= nrows; i += kSlabThreads) s_rs[i] = rs[row_lo + i] - pos_lo;
+    for (int i = threadIdx.x; i < pos_hi - pos_lo; i += kSlabThreads) {
+      s_cand[i] = b.cand[pos_lo + i];
+      s_col[i] = (uint8_t)b.scol[pos_lo + i];
+    }
+    __syncthreads();
+  }
+  RowsStaged sv{s_mask, s_rs, s_cand, s_col, row_lo};
+  RowsGlobal gv{b.row_mask + 2 * rbase, rs, b.cand, b.scol};
+  const int64_t es = b.offsets[e];
+  for (int p = q_lo + (int)threadIdx.x; p < q_hi; p += kSlabThreads) {
+    const int i = b.sorted[p];
+    const int64_t gi = es + i;
+    if (b.key[gi] < 0) continue;
+    const int li = b.layer[gi];
+    int lo, hi;
+    layer_window(li, sib, P.n_layers, kDensity ? 0 : 1, &lo, &hi);
+    const bool inside = staged && lo * kEtaBins >= row_lo && hi * kEtaBins + kEtaBins <= row_hi;
+    const float phi_i = b.phi[gi], zi = b.z[gi];
+    const int eb = eta_bin(b.eta[gi], P), pb = phi_bin(phi_i, P);
+    const float r0 = __fmul_rn(b.roa[gi], zi);
+    if (kDensity) {
+      const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
+      const float rho = inside ? density_of(sv, P, li, eb, pb, phi_i, zi, r0, thr, p - pos_lo)
+                               : density_of(gv, P, li, eb, pb, phi_i, zi, r0, thr, p);
+      b.rho[gi] = rho;
+      reinterpret_cast<float*>(b.cand)[4 * (int64_t)p + 3] = rho;
+    } else {
+      const float rho_i = b.rho[gi];
+      Nh3 o = inside ? nearest_higher_of(sv, P, li, eb, pb, phi_i, zi, r0, rho_i)
+                     : nearest_higher_of(gv, P, li, eb, pb, phi_i, zi, r0, rho_i);
+      if (o.nq >= 0 && inside) o.nq += pos_lo;
+      if (o.best != FLT_MAX) {
+        b.delta_t[gi] = o.best_t;
+        b.delta_l[gi] = o.best_l;
+        b.nh_l[gi] = o.nl;
+        b.nh_i[gi] = b.sorted[o.nq];
+      } else {
+        b.delta_t[gi] = FLT_MAX;
+        b.delta_l[gi] = INT_MAX;
+        b.nh_l[gi] = -1;
+        b.nh_i[gi] = -1;
+      }
+    }
   }
 }
 
@@ -448,13 +538,16 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
     NvtxRange r("clue3d/row_sort");
     k3_row_sort<<<grid, T, 0, s>>>(b);
   }
+  const int n_slabs = (p.n_layers + kSlabLayers - 1) / kSlabLayers;
+  const int64_t slab_blocks = (int64_t)b.n_events * n_slabs;
+  if (slab_blocks > INT32_MAX) return cudaErrorInvalidValue;
   {
     NvtxRange r("clue3d/density");
-    k3_density<<<grid, T, 0, s>>>(b, p);
+    k3_search<true><<<(unsigned)slab_blocks, kSlabThreads, 0, s>>>(b, p, n_slabs);
   }
   {
     NvtxRange r("clue3d/nearest_higher");
-    k3_nh<<<grid, T, 0, s>>>(b, p);
+    k3_search<false><<<(unsigned)slab_blocks, kSlabThreads, 0, s>>>(b, p, n_slabs);
   }
   {
     NvtxRange r("clue3d/flags");

@@ -30,17 +30,7 @@ namespace {
 constexpr double kWScale = 16777216.0;  // 2^24
 constexpr double kPScale = 65536.0;     // 2^16
 
-enum BridgeSlot { B_OFF, B_COFF, B_COUNT, B_ACC, B_SEED, B_LZ, B_FLAGS, B_SLOTS };
-
-__device__ __forceinline__ int32_t event_of(const int64_t* __restrict__ off, int32_t E, int64_t i) {
-  int32_t lo = 0, hi = E;  // largest e < E with off[e] <= i
-  while (hi - lo > 1) {
-    const int32_t mid = (lo + hi) >> 1;
-    if (off[mid] <= i) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
+enum BridgeSlot { B_OFF, B_COFF, B_COUNT, B_ACC, B_SEED, B_LZ, B_FLAGS, B_CEV, B_SLOTS };
 
 // Points per block of the point kernels: each block finds the event of its
 // first point once and then follows event boundaries forwards.
@@ -86,82 +76,128 @@ __device__ __forceinline__ unsigned long long fx_pos(float w, float v) {
   return ((uw ^ uv) >> 31) ? (0ull - q) : q;
 }
 
-__global__ void __launch_bounds__(kBridgeThreads) k_bridge_count(int32_t E, int64_t N,
-                                                                   const int64_t* __restrict__ off,
+// Points of a thread per round (loads of a round are issued together).
+constexpr int kBridgePer = 8;
+constexpr int kBridgeRounds = kBridgeChunk / (kBridgeThreads * kBridgePer);
+static_assert(kBridgeRounds * kBridgeThreads * kBridgePer == kBridgeChunk, "chunk layout");
+
+__global__ void __launch_bounds__(kBridgeThreads) k_bridge_count(int64_t N, const int64_t* __restrict__ off,
+                                                                   const int32_t* __restrict__ chunk_ev,
                                                                    const int32_t* __restrict__ seed,
                                                                    int32_t* __restrict__ counts) {
-  __shared__ int32_t s_e;
   const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
-  if (threadIdx.x == 0) s_e = event_of(off, E, c0);
-  __syncthreads();
-  int32_t e = s_e;
-  for (int k = 0; k < kBridgeChunk / kBridgeThreads; ++k) {
-    const int64_t i = c0 + (int64_t)k * kBridgeThreads + threadIdx.x;
-    int32_t key = -1;
-    if (i < N) {
-      while (off[e + 1] <= i) ++e;  // i grows with k
-      if (seed[i]) key = e;
+  int32_t e = chunk_ev[blockIdx.x];
+  int64_t next = off[e + 1];  // first point after event e
+  for (int rd = 0; rd < kBridgeRounds; ++rd) {
+    const int64_t i0 = c0 + (int64_t)rd * kBridgeThreads * kBridgePer + threadIdx.x;
+    int32_t sv[kBridgePer];
+#pragma unroll
+    for (int j = 0; j < kBridgePer; ++j) {
+      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
+      sv[j] = i < N ? seed[i] : 0;
     }
-    // one increment per event among the warp's seeds
-    const unsigned grp = __match_any_sync(0xffffffffu, key);
-    if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[key], __popc(grp));
-  }
-}
-
-// The sums of a cluster are exact integers, so they may be added in any
-// grouping: lanes holding the same cluster in a run of consecutive lanes (the
-// usual case: a cluster's points are mostly consecutive) add theirs first and
-// the run's last lane makes the three atomic additions.
-__global__ void __launch_bounds__(kBridgeThreads) k_bridge_accumulate(
-    int32_t E, int64_t N, const int64_t* __restrict__ off, const int64_t* __restrict__ coff,
-    const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ w,
-    const int32_t* __restrict__ seed, const int32_t* __restrict__ ci, unsigned long long* __restrict__ acc,
-    int32_t* __restrict__ seed_of, int32_t* __restrict__ flags) {
-  __shared__ int32_t s_e;
-  const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
-  if (threadIdx.x == 0) s_e = event_of(off, E, c0);
-  __syncthreads();
-  int32_t e = s_e;
-  const int lane = threadIdx.x & 31;
-  for (int k = 0; k < kBridgeChunk / kBridgeThreads; ++k) {
-    const int64_t i = c0 + (int64_t)k * kBridgeThreads + threadIdx.x;
-    int32_t g = -1;
-    unsigned long long v0 = 0, v1 = 0, v2 = 0;
-    if (i < N) {
-      while (off[e + 1] <= i) ++e;  // i grows with k
-      const int32_t c = ci[i];
-      if (c >= 0) {
-        if (c >= coff[e + 1] - coff[e]) {
-          atomicExch(&flags[kFlagError], 1);
+#pragma unroll
+    for (int j = 0; j < kBridgePer; ++j) {
+      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
+      int32_t key = -1;
+      if (i < N) {
+        while (next <= i) next = off[++e + 1];  // i grows with (rd, j)
+        if (sv[j]) key = e;
+      }
+      // one increment per event among the warp's seeds
+      const unsigned any = __ballot_sync(0xffffffffu, key >= 0);
+      if (any) {
+        const int k0 = __shfl_sync(0xffffffffu, key, __ffs(any) - 1);
+        if (__all_sync(0xffffffffu, key < 0 || key == k0)) {
+          if ((threadIdx.x & 31) == __ffs(any) - 1) atomicAdd(&counts[k0], __popc(any));
         } else {
-          g = (int32_t)(coff[e] + c);
-          const float wi = w[i];
-          v0 = fx_weight(wi);
-          v1 = fx_pos(wi, x[i]);
-          v2 = fx_pos(wi, y[i]);
-          if (seed[i]) seed_of[g] = (int32_t)i;
+          const unsigned grp = __match_any_sync(0xffffffffu, key);
+          if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[key], __popc(grp));
         }
       }
     }
-    const int32_t gp = __shfl_up_sync(0xffffffffu, g, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || gp != g);
-    const int first = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // the run's first lane
+  }
+}
+
+// Sum of a 64-bit value over the lanes of `grp` (lanes holding the same
+// cluster), exact modulo 2^64: three 22-bit limbs, each summed with one
+// 32-bit reduction (32 lanes x 2^22 < 2^32), then put back together.
+__device__ __forceinline__ unsigned long long group_sum(unsigned grp, unsigned long long v) {
+  const unsigned l0 = __reduce_add_sync(grp, (unsigned)(v & 0x3fffffu));
+  const unsigned l1 = __reduce_add_sync(grp, (unsigned)((v >> 22) & 0x3fffffu));
+  const unsigned l2 = __reduce_add_sync(grp, (unsigned)(v >> 44));
+  return (unsigned long long)l0 + ((unsigned long long)l1 << 22) + ((unsigned long long)l2 << 44);
+}
+
+// The sums of a cluster are exact integers, so they may be added in any
+// grouping: the lanes of a warp holding the same cluster add theirs first and
+// one of them makes the three atomic additions.
+__global__ void __launch_bounds__(kBridgeThreads) k_bridge_accumulate(
+    int64_t N, const int64_t* __restrict__ off, const int32_t* __restrict__ chunk_ev,
+    const int64_t* __restrict__ coff, const float* __restrict__ x, const float* __restrict__ y,
+    const float* __restrict__ w, const int32_t* __restrict__ seed, const int32_t* __restrict__ ci,
+    unsigned long long* __restrict__ acc, int32_t* __restrict__ seed_of, int32_t* __restrict__ flags) {
+  const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
+  int32_t e = chunk_ev[blockIdx.x];
+  int64_t next = off[e + 1];  // first point after event e
+  int64_t cbase = coff[e], ccount = coff[e + 1] - cbase;
+  const int lane = threadIdx.x & 31;
+  for (int rd = 0; rd < kBridgeRounds; ++rd) {
+    const int64_t i0 = c0 + (int64_t)rd * kBridgeThreads * kBridgePer + threadIdx.x;
+    int32_t cv[kBridgePer], sv[kBridgePer];
+    float wv[kBridgePer], xv[kBridgePer], yv[kBridgePer];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long t0 = __shfl_up_sync(0xffffffffu, v0, o);
-      const unsigned long long t1 = __shfl_up_sync(0xffffffffu, v1, o);
-      const unsigned long long t2 = __shfl_up_sync(0xffffffffu, v2, o);
-      if (lane - o >= first) {
-        v0 += t0;
-        v1 += t1;
-        v2 += t2;
-      }
+    for (int j = 0; j < kBridgePer; ++j) {
+      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
+      cv[j] = i < N ? ci[i] : -1;
     }
-    const int32_t gn = __shfl_down_sync(0xffffffffu, g, 1);
-    if (g >= 0 && (lane == 31 || gn != g)) {
-      atomicAdd(&acc[3 * (int64_t)g], v0);
-      atomicAdd(&acc[3 * (int64_t)g + 1], v1);
-      atomicAdd(&acc[3 * (int64_t)g + 2], v2);
+#pragma unroll
+    for (int j = 0; j < kBridgePer; ++j) {
+      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
+      const bool in = cv[j] >= 0;
+      wv[j] = in ? w[i] : 0.f;
+      xv[j] = in ? x[i] : 0.f;
+      yv[j] = in ? y[i] : 0.f;
+      sv[j] = in ? seed[i] : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < kBridgePer; ++j) {
+      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
+      int32_t g = -1;
+      unsigned long long v0 = 0, v1 = 0, v2 = 0;
+      if (i < N) {
+        if (next <= i) {  // i grows with (rd, j)
+          while (next <= i) next = off[++e + 1];
+          cbase = coff[e];
+          ccount = coff[e + 1] - cbase;
+        }
+        const int32_t c = cv[j];
+        if (c >= 0) {
+          if (c >= ccount) {
+            atomicExch(&flags[kFlagError], 1);
+          } else {
+            g = (int32_t)(cbase + c);
+            v0 = fx_weight(wv[j]);
+            v1 = fx_pos(wv[j], xv[j]);
+            v2 = fx_pos(wv[j], yv[j]);
+            if (sv[j]) seed_of[g] = (int32_t)i;
+          }
+        }
+      }
+      // a warp whose lanes all hold one cluster (the usual case) reduces with
+      // the full mask; otherwise the lanes are grouped by cluster first
+      const int32_t g0 = __shfl_sync(0xffffffffu, g, 0);
+      const unsigned grp = __all_sync(0xffffffffu, g == g0) ? 0xffffffffu : __match_any_sync(0xffffffffu, g);
+      if (g >= 0) {
+        v0 = group_sum(grp, v0);
+        v1 = group_sum(grp, v1);
+        v2 = group_sum(grp, v2);
+        if (lane == __ffs(grp) - 1) {
+          atomicAdd(&acc[3 * (int64_t)g], v0);
+          atomicAdd(&acc[3 * (int64_t)g + 1], v1);
+          atomicAdd(&acc[3 * (int64_t)g + 2], v2);
+        }
+      }
     }
   }
 }
@@ -215,6 +251,17 @@ int check_offsets(int32_t E, const int64_t* off, const char* what) {
   return CLUE_OK;
 }
 
+// Event of the first point of each chunk of kBridgeChunk points (empty
+// events own no point; the event of a point is the last e with off[e] <= i).
+void chunk_events(int32_t E, const int64_t* off, int nch, int32_t* cev) {
+  int32_t e = 0;
+  for (int c = 0; c < nch; ++c) {
+    const int64_t i = (int64_t)c * kBridgeChunk;
+    while (e + 1 < E && off[e + 1] <= i) ++e;
+    cev[c] = e;
+  }
+}
+
 int grid_for(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
 }
@@ -250,17 +297,23 @@ int clue_bridge_count(clue_handle* hh, int32_t E, const int64_t* off, const int3
     std::vector<size_t> need(clue::B_SLOTS, 0);
     need[clue::B_OFF] = 8 * (size_t)(E + 1);
     need[clue::B_COUNT] = 4 * (size_t)E;
+    const int nch = clue::chunks_for(N);
+    need[clue::B_CEV] = 4 * (size_t)std::max(nch, 1);
     if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
-    if ((rc = h->stage.reserve(8 * (size_t)(E + 1)))) return rc;
+    if ((rc = h->stage.reserve(8 * (size_t)(E + 1) + 4 * (size_t)nch))) return rc;
     auto P = [&](int s) { return h->arena_bridge.ptr(s); };
     cudaStream_t s = h->stream;
     memcpy(h->stage.p, off, 8 * (size_t)(E + 1));
+    int32_t* cev = reinterpret_cast<int32_t*>(static_cast<char*>(h->stage.p) + 8 * (size_t)(E + 1));
+    clue::chunk_events(E, off, nch, cev);
     if ((e = cudaMemcpyAsync(P(clue::B_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(P(clue::B_CEV), cev, 4 * (size_t)nch, cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemsetAsync(P(clue::B_COUNT), 0, 4 * (size_t)E, s)))
       return cuda_error(e, "bridge set-up");
     if (N > 0)
-      clue::k_bridge_count<<<clue::chunks_for(N), clue::kBridgeThreads, 0, s>>>(E, N, static_cast<const int64_t*>(P(clue::B_OFF)),
-                                                              isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
+      clue::k_bridge_count<<<nch, clue::kBridgeThreads, 0, s>>>(N, static_cast<const int64_t*>(P(clue::B_OFF)),
+                                                                  static_cast<const int32_t*>(P(clue::B_CEV)),
+                                                                  isSeed, static_cast<int32_t*>(P(clue::B_COUNT)));
     if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_count");
     std::vector<int32_t> counts(E);
     if ((e = cudaMemcpyAsync(counts.data(), P(clue::B_COUNT), 4 * (size_t)E, cudaMemcpyDeviceToHost, s)) ||
@@ -300,8 +353,10 @@ int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, c
     need[clue::B_SEED] = 4 * (size_t)std::max<int64_t>(C, 1);
     need[clue::B_LZ] = 4 * (size_t)p->n_layers;
     need[clue::B_FLAGS] = 4 * clue::kFlagCount;
+    const int nch = clue::chunks_for(N);
+    need[clue::B_CEV] = 4 * (size_t)std::max(nch, 1);
     if ((rc = h->arena_bridge.reserve(need, clue::bridge_budget(h)))) return rc;
-    const size_t stage_bytes = 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers;
+    const size_t stage_bytes = 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers + 4 * (size_t)nch;
     if ((rc = h->stage.reserve(stage_bytes))) return rc;
     if ((rc = h->flags_host.reserve(4 * clue::kFlagCount))) return rc;
     auto P = [&](int s) { return h->arena_bridge.ptr(s); };
@@ -309,6 +364,8 @@ int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, c
     memcpy(st, off, 8 * (size_t)(E + 1));
     memcpy(st + 8 * (size_t)(E + 1), coff, 8 * (size_t)(E + 1));
     memcpy(st + 16 * (size_t)(E + 1), p->layer_z, 4 * (size_t)p->n_layers);
+    int32_t* cev = reinterpret_cast<int32_t*>(st + 16 * (size_t)(E + 1) + 4 * (size_t)p->n_layers);
+    clue::chunk_events(E, off, nch, cev);
     cudaStream_t s = h->stream;
     if ((e = cudaMemcpyAsync(P(clue::B_OFF), st, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemcpyAsync(P(clue::B_COFF), st + 8 * (size_t)(E + 1), 8 * (size_t)(E + 1), cudaMemcpyHostToDevice,
@@ -317,15 +374,16 @@ int clue_bridge_build(clue_handle* hh, const clue_bridge_params* p, int32_t E, c
                              cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemsetAsync(P(clue::B_ACC), 0, 24 * (size_t)std::max<int64_t>(C, 1), s)) ||
         (e = cudaMemsetAsync(P(clue::B_SEED), 0, 4 * (size_t)std::max<int64_t>(C, 1), s)) ||
-        (e = cudaMemsetAsync(P(clue::B_FLAGS), 0, 4 * clue::kFlagCount, s)))
+        (e = cudaMemsetAsync(P(clue::B_FLAGS), 0, 4 * clue::kFlagCount, s)) ||
+        (e = cudaMemcpyAsync(P(clue::B_CEV), cev, 4 * (size_t)nch, cudaMemcpyHostToDevice, s)))
       return cuda_error(e, "bridge set-up");
     int32_t* flags = static_cast<int32_t*>(P(clue::B_FLAGS));
     auto* acc = static_cast<unsigned long long*>(P(clue::B_ACC));
     auto* seed_of = static_cast<int32_t*>(P(clue::B_SEED));
     if (N > 0)
-      clue::k_bridge_accumulate<<<clue::chunks_for(N), clue::kBridgeThreads, 0, s>>>(
-          E, N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int64_t*>(P(clue::B_COFF)), x, y,
-          weight, isSeed, clusterIndex, acc, seed_of, flags);
+      clue::k_bridge_accumulate<<<nch, clue::kBridgeThreads, 0, s>>>(
+          N, static_cast<const int64_t*>(P(clue::B_OFF)), static_cast<const int32_t*>(P(clue::B_CEV)),
+          static_cast<const int64_t*>(P(clue::B_COFF)), x, y, weight, isSeed, clusterIndex, acc, seed_of, flags);
     if ((e = cudaGetLastError())) return cuda_error(e, "k_bridge_accumulate");
     if (C > 0)
       clue::k_bridge_finalize<<<clue::grid_for(C), 256, 0, s>>>(C, acc, seed_of, x, y, layer,

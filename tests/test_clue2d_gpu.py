@@ -329,6 +329,7 @@ def test_graph_only_for_repeated_shapes(cuda_lib):
     for i in (0, 1, 0, 0, 0, 1, 1, 1):  # direct, direct, direct, capture, replay, direct, capture, replay
         for v in outs[i].values():
             v.zero_()
+        torch.cuda.synchronize()  # the handle runs on its own stream: the fill must be done first
         algo.run_batch(bs[i]["offsets"], dev[i]["x"], dev[i]["y"], dev[i]["layer"], dev[i]["weight"], out=outs[i],
                        flags=C.DEVICE_MEMORY)
         algo.synchronize()

@@ -77,6 +77,7 @@ def test_uneven_4096_device_resident_every_event(uneven, cuda_lib):
     for rep in range(3):  # direct launches, capture, graph replay
         for v in out.values():
             v.fill_(-7)
+        torch.cuda.synchronize()  # the handle runs on its own stream: the fill must be done first
         algo.run_batch(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY)
         algo.synchronize()
         assert_bitexact(_host(out), want, KEYS_2D, label=f"4096 events, device resident, run {rep}")
@@ -108,6 +109,7 @@ def test_hgcal_1000_batched_and_plain_every_event(hgcal, cuda_lib):
     for flags, label in ((0, "batched"), (C.PLAIN, "plain")):
         for v in out.values():
             v.fill_(-7)
+        torch.cuda.synchronize()  # the handle runs on its own stream: the fill must be done first
         algo.run_batch(b["offsets"], d["x"], d["y"], d["layer"], d["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
         algo.synchronize()
         assert_bitexact(_host(out), want, KEYS_2D, label=f"1,000 HGCAL events, {label}")

@@ -42,6 +42,7 @@ def _call(torch, dev, stream, out=None):
         out = {k: torch.full((n,), -7, dtype=torch.float32 if k in ("rho", "delta") else torch.int32, device="cuda")
                for k in KEYS}
     o = C.outputs_struct(out)
+    torch.cuda.synchronize()  # the fill above ran on torch's stream, the call runs on `stream`
     rc = C.lib().clue_run_event_noalloc(ctypes.byref(C.Params(*PRM)), n, dev["x"].data_ptr(), dev["y"].data_ptr(),
                                         dev["layer"].data_ptr(), dev["weight"].data_ptr(), ctypes.byref(o),
                                         stream.cuda_stream)
