@@ -73,11 +73,6 @@ __device__ __forceinline__ int chunk_event(const int32_t* chunk_start, int n_eve
   return lo;
 }
 
-// Layer of point i: from the one-byte copy when the batch has one.
-__device__ __forceinline__ int layer_at(const Batch2D& b, int64_t i) {
-  return b.layer8 ? (int)b.layer8[i] : b.layer[i];
-}
-
 // Event of a chunk: from the host-built table when the batch has one.
 __device__ __forceinline__ int event_of_chunk(const Batch2D& b, int c) {
   return b.chunk_ev ? b.chunk_ev[c] : chunk_event(b.chunk_start, b.n_events, c);
@@ -631,7 +626,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int64_t i = i0 + threadIdx.x + (int64_t)j * kChunkThreads;
-    lv[j] = i < i1 ? layer_at(b, i) : 0;
+    lv[j] = i < i1 ? b.layer[i] : 0;
   }
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
@@ -650,7 +645,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_count(Batch2D b) {
     // predecessor of lane 0 is read from memory, the others by shuffle)
     const int prev = __shfl_up_sync(0xffffffffu, l, 1);
     if (key >= 0 && i > es) {
-      const int pl = lane ? prev : layer_at(b, i - 1);
+      const int pl = lane ? prev : b.layer[i - 1];
       if (l < pl) ungrouped = true;
     }
     // most warps of grouped input hold one layer: one increment for the warp
@@ -755,7 +750,7 @@ __global__ void __launch_bounds__(kChunkThreads) k_scatter(Batch2D b) {
     const int64_t i = base + threadIdx.x;
     int key = -1;
     if (i < i1) {
-      const int l = layer_at(b, i);
+      const int l = b.layer[i];
       if (l >= 0 && l < kLayers) key = e * kLayers + l;
     }
     const unsigned mask = __match_any_sync(0xffffffffu, key);

@@ -82,7 +82,6 @@ struct Batch2D {
   const float* x = nullptr;
   const float* y = nullptr;
   const int32_t* layer = nullptr;
-  const uint8_t* layer8 = nullptr;  // when set, the layers as one byte each (255: invalid) instead of `layer`
   const float* w = nullptr;
   float* rho = nullptr;
   float* delta = nullptr;

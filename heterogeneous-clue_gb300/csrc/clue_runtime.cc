@@ -15,7 +15,6 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "../../include/clue.h"
@@ -197,8 +196,6 @@ size_t arena_bytes_after_2d(const Handle* h, int32_t E, int64_t N, int64_t nchun
 Handle::~Handle() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (done_event) cudaEventDestroy(done_event);
-  for (auto ev : sub_done)
-    if (ev) cudaEventDestroy(ev);
   for (auto ev : pipe_events)
     if (ev) cudaEventDestroy(ev);
   if (copy_in) cudaStreamDestroy(copy_in);
@@ -616,45 +613,7 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
   }
   if ((rc = h->stage.reserve(st_off[S]))) return rc;
   if ((rc = h->flags_host.reserve(4 * kFlagCount * (size_t)S))) return rc;
-  if ((rc = h->stage_layer.reserve((size_t)r.N))) return rc;
   cudaError_t e;
-  while ((int)h->sub_done.size() < S) {
-    cudaEvent_t ev = nullptr;
-    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
-      return cuda_error(e, "cudaEventCreate");
-    h->sub_done.push_back(ev);
-  }
-  // Host passes on resident helpers: the layers go over the link as one byte
-  // each (an int32 layer outside [0, 100) becomes 255, which the device
-  // reports like any invalid layer), and isSeed does not come back at all:
-  // the host applies the reference's seed rule, delta > dc && rho >= rhoc
-  // (src/serial/plugin-CLUEClusterizer/CLUEAlgoKernels.h:114-131), to the rho
-  // and delta it receives -- the device's own rule on the same values, so the
-  // flag is the one the device computed.  4 + 3 of the 36 bytes per point.
-  if (!h->pool.started()) h->pool.start((int)std::min(15u, std::max(3u, std::thread::hardware_concurrency()) - 1));
-  uint8_t* l8 = static_cast<uint8_t*>(h->stage_layer.p);
-  constexpr int64_t kHostPiece = int64_t(1) << 18;  // points per host piece
-  auto pieces = [&](int64_t n) { return (size_t)((n + kHostPiece - 1) / kHostPiece); };
-  auto narrow_layers = [&](int64_t p0, int64_t n) {
-    h->pool.for_pieces(pieces(n), [&](size_t j) {
-      const int64_t a = p0 + (int64_t)j * kHostPiece, z = std::min(a + kHostPiece, p0 + n);
-      const int32_t* src = r.layer;
-      for (int64_t q = a; q < z; ++q) {
-        const int32_t l = src[q];
-        l8[q] = (l >= 0 && l < kLayers) ? (uint8_t)l : (uint8_t)0xff;
-      }
-    });
-  };
-  const float dc = h->p2d.dc, rhoc = h->p2d.rhoc;
-  auto seed_flags = [&](int64_t p0, int64_t n) {
-    h->pool.for_pieces(pieces(n), [&](size_t j) {
-      const int64_t a = p0 + (int64_t)j * kHostPiece, z = std::min(a + kHostPiece, p0 + n);
-      const float* rho = r.out->rho;
-      const float* delta = r.out->delta;
-      int32_t* seed = r.out->isSeed;
-      for (int64_t q = a; q < z; ++q) seed[q] = (delta[q] > dc && rho[q] >= rhoc) ? 1 : 0;
-    });
-  };
   for (auto* st : {&h->copy_in, &h->copy_out}) {
     if (!*st && (e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking)) != cudaSuccess) {
       *st = nullptr;
@@ -677,18 +636,6 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
       return cuda_error(e, "cudaEventRecord");
   int32_t* fh = static_cast<int32_t*>(h->flags_host.p);
   int64_t kernels = 0;
-  int filled = 0;  // sub-batches whose isSeed the host has written
-  auto fill_seeds = [&](int queued, bool wait) -> int {
-    while (filled < queued) {
-      const cudaError_t q = wait ? cudaEventSynchronize(h->sub_done[filled]) : cudaEventQuery(h->sub_done[filled]);
-      if (q == cudaErrorNotReady) return CLUE_OK;
-      if (q != cudaSuccess) return cuda_error(q, "pipelined batch");
-      const int64_t a = r.off[cut[filled]];
-      seed_flags(a, r.off[cut[filled + 1]] - a);
-      ++filled;
-    }
-    return CLUE_OK;
-  };
   for (int i = 0; i < S; ++i) {
     const int k = i % kPipeSlots;
     const int32_t e0 = cut[i], Es = cut[i + 1] - e0;
@@ -710,8 +657,6 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
     Batch2D b;
     fill_batch_views(h, sub, sc[Es], true, b, slot_arena[k]);
     const size_t n4 = 4 * (size_t)Ns;
-    narrow_layers(p0, Ns);
-    b.layer8 = reinterpret_cast<const uint8_t*>(b.layer);  // the slot's layer buffer holds the bytes
     // kernels of both slots stay on the handle's stream: letting the next
     // sub-batch's persistent kernel start beside the draining one measured slower
     cudaStream_t ci = h->copy_in, co = h->copy_out, cs = h->stream;
@@ -723,7 +668,7 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
             cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.x, r.x + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.y, r.y + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
-        (e = cudaMemcpyAsync((void*)b.layer8, l8 + p0, (size_t)Ns, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
+        (e = cudaMemcpyAsync((void*)b.layer, r.layer + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
         (e = cudaMemcpyAsync((void*)b.w, r.w + p0, n4, cudaMemcpyHostToDevice, ci)) != cudaSuccess ||
         (e = cudaEventRecord(h2d[k], ci)) != cudaSuccess)
       return cuda_error(e, "H2D sub-batch");
@@ -739,17 +684,15 @@ int run_2d_pipelined(Handle* h, const Run2D& r) {
         (e = cudaMemcpyAsync(o->rho + p0, b.rho, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
         (e = cudaMemcpyAsync(o->delta + p0, b.delta, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
         (e = cudaMemcpyAsync(o->nearestHigher + p0, b.nh, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o->isSeed + p0, b.seed, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
         (e = cudaMemcpyAsync(o->clusterIndex + p0, b.ci, n4, cudaMemcpyDeviceToHost, co)) != cudaSuccess ||
         (e = cudaMemcpyAsync(fh + kFlagCount * (size_t)i, b.flags, 4 * kFlagCount, cudaMemcpyDeviceToHost, co)) !=
             cudaSuccess ||
-        (e = cudaEventRecord(d2h[k], co)) != cudaSuccess || (e = cudaEventRecord(h->sub_done[i], co)) != cudaSuccess)
+        (e = cudaEventRecord(d2h[k], co)) != cudaSuccess)
       return cuda_error(e, "D2H sub-batch");
-    // seed flags of sub-batches already copied back, while later ones run
-    if ((rc = fill_seeds(i + 1, false))) return rc;
   }
-  if ((rc = fill_seeds(S, true))) return rc;
-  h->last_run.h2d_bytes = 13 * r.N + 12 * (int64_t)(r.E + S) + 4 * n_chunks_of(r.E, r.off);
-  h->last_run.d2h_bytes = 16 * r.N + 4 * kFlagCount * (int64_t)S;
+  h->last_run.h2d_bytes = 16 * r.N + 12 * (int64_t)(r.E + S) + 4 * n_chunks_of(r.E, r.off);
+  h->last_run.d2h_bytes = 20 * r.N + 4 * kFlagCount * (int64_t)S;
   h->last_run.kernel_launches = kernels;
   // the handle's stream orders after the last copy-out, so later work and
   // clue_synchronize see a finished batch

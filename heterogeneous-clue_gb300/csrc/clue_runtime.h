@@ -11,7 +11,6 @@
 
 #include "../../include/clue.h"
 #include "clue_internal.h"
-#include "copy_pool.h"
 
 namespace clue {
 
@@ -124,9 +123,6 @@ struct Handle {
   clue_run_stats last_run{};              // copies and kernels of the last 2D run
   int64_t graph_kernels = 0;              // kernels in graph_exec
   PinnedBuf stage;
-  PinnedBuf stage_layer;                  // pipelined host-memory path: layers as one byte each
-  std::vector<cudaEvent_t> sub_done;      // pipelined host-memory path: outputs of sub-batch i copied back
-  CopyPool pool;                          // pipelined host-memory path: host passes (started at first use)
   PinnedBuf flags_host;
   PinnedBuf nt_host;
   cudaGraphExec_t graph_exec = nullptr;

@@ -94,7 +94,7 @@ def test_uneven_4096_pinned_host_memory_every_event(uneven, cuda_lib):
             for k in KEYS_2D}
     algo.run_batch(b["offsets"], hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
     st = algo.last_run_stats()
-    assert st["h2d_bytes"] >= 13 * n and st["d2h_bytes"] >= 16 * n
+    assert st["h2d_bytes"] >= 16 * n and st["d2h_bytes"] >= 20 * n
     assert_bitexact({k: v.numpy() for k, v in hout.items()}, want, KEYS_2D, label="4096 events, pinned host")
     algo.close()
 
