@@ -575,15 +575,19 @@ def run_gb300(args):
         for _ in range(max(1, args.warmup)):
             algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
         barrier()
+        step_ms = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            t1 = time.perf_counter()
             algo.run_batch(off, hin["x"], hin["y"], hin["layer"], hin["weight"], out=hout)
+            step_ms.append(1000 * (time.perf_counter() - t1))
         dt = max_over_ranks(time.perf_counter() - t0)
         st = algo.last_run_stats()  # the copies as the library made them
         h2d_bytes, d2h_bytes = st["h2d_bytes"], st["d2h_bytes"]
         e2e = {"value": ws * E * args.steps / dt, "unit": "events/s",
                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
-               "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps}
+               "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps,
+               "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)]}
         del hin, hout
 
     # the legs below use handles of their own: release the main one's buffers

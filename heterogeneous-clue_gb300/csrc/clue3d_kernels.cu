@@ -163,7 +163,7 @@ __global__ void k3_scatter(Batch3D b) {
 }
 
 // Each entry's rank inside its row by (column, index) gives its final slot.
-__global__ void k3_row_sort(Batch3D b) {
+__global__ void k3_row_sort(Batch3D b, Params3D P) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= b.n_points) return;
   const int e = event_of(b.offsets, b.n_events, p);
@@ -183,6 +183,14 @@ __global__ void k3_row_sort(Batch3D b) {
   // from the density search)
   const int64_t gi = b.offsets[e] + idx;
   b.cand[s + rank] = make_float4(b.roa[gi], b.phi[gi], b.energy[gi], 0.f);
+  // and what a search needs of the entry as a query, so that the searches
+  // read their queries in sorted order instead of gathering them
+  if (k >= 0) {
+    const float zi = b.z[gi];
+    const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
+    const int bins = b.layer[gi] | (eta_bin(b.eta[gi], P) << 11) | (phi_bin(b.phi[gi], P) << 17);
+    b.qrec[s + rank] = make_float4(zi, __fmul_rn(b.roa[gi], zi), thr, __int_as_float(bins));
+  }
   // occupancy of the row's phi columns; bit 127 marks a column held twice
   unsigned long long* m = b.row_mask + 2 * r;
   const unsigned long long bit = 1ull << (col & 63);
@@ -257,11 +265,26 @@ __device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long l
   return __popcll(m0) + __popcll(m1 & ((1ull << (p - 64)) - 1));
 }
 
-// visit_row() for row r through its occupancy mask: the row start is read
+// Phi columns of the window [pb - d, pb + d] modulo 126 as a 126-bit mask
+// (the reference's iphi = iphi_it mod nPhiBins, CLUE3DAlgoKernels.h:80-84).
+struct ColMask {
+  unsigned long long w0 = 0, w1 = 0;
+  __device__ __forceinline__ ColMask(int pb, int d) {
+    for (int c = pb - d; c <= pb + d; ++c) {
+      const int cc = c < 0 ? c + kPhiBins : (c >= kPhiBins ? c - kPhiBins : c);
+      if (cc < 64) w0 |= 1ull << cc; else w1 |= 1ull << (cc - 64);
+    }
+  }
+};
+
+// visit_row() for row r through its occupancy mask: a row with no entry in
+// the window's columns is skipped on the mask alone, the row start is read
 // only when the window holds an entry, and the row is not scanned.
 template <class V, class F>
-__device__ __forceinline__ void visit_row_masked(const V& v, int r, int p0, int p1, F&& f) {
+__device__ __forceinline__ void visit_row_masked(const V& v, int r, const ColMask& wm, int p0, int p1, F&& f) {
   const unsigned long long m0 = v.m0(r), m1 = v.m1(r);
+  // bit 127 of m1 marks a repeated column; the window never holds column 127
+  if (((m0 & wm.w0) | (m1 & wm.w1)) == 0) return;
   if (m1 >> 63) {  // a column holds several entries: walk the row
     visit_row(v, v.start(r), v.start(r + 1), p0, p1, f);
     return;
@@ -289,13 +312,14 @@ __device__ __forceinline__ float density_of(const V& v, const Params3D& P, int l
                                             float zi, float r0, float thr, int self) {
   int lo, hi;
   layer_window(li, P.dens_sib, P.n_layers, 0, &lo, &hi);
+  const ColMask wm(pb, 2);
   float rho = 0.f;
   for (int cl = lo; cl <= hi; ++cl) {
     const bool same = (cl == li);
     const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
     const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
-      visit_row_masked(v, cl * kEtaBins + ie, pb - 2, pb + 2, [&](int q) {
+      visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 2, pb + 2, [&](int q) {
         const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
         const float r1 = __fmul_rn(cj.x, zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
@@ -322,12 +346,13 @@ __device__ __forceinline__ Nh3 nearest_higher_of(const V& v, const Params3D& P, 
                                                  float zi, float r0, float rho_i) {
   int lo, hi;
   layer_window(li, P.nh_sib, P.n_layers, 1, &lo, &hi);
+  const ColMask wm(pb, 1);
   Nh3 o;
   for (int cl = lo; cl <= hi; ++cl) {
     if (!P.nh_same && cl == li) continue;
     const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
     for (int ie = e0; ie <= e1; ++ie) {
-      visit_row_masked(v, cl * kEtaBins + ie, pb - 1, pb + 1, [&](int q) {
+      visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 1, pb + 1, [&](int q) {
         const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
         const float r1 = __fmul_rn(cj.x, zi);
         const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
@@ -399,24 +424,25 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
   RowsGlobal gv{b.row_mask + 2 * rbase, rs, b.cand, b.scol};
   const int64_t es = b.offsets[e];
   for (int p = q_lo + (int)threadIdx.x; p < q_hi; p += kSlabThreads) {
-    const int i = b.sorted[p];
-    const int64_t gi = es + i;
-    if (b.key[gi] < 0) continue;
-    const int li = b.layer[gi];
+    // the query rows hold only accepted clusters (rejected ones are in the
+    // event's last row); a query's own data is read in sorted order
+    const float4 qr = b.qrec[p];
+    const float4 cr = staged ? s_cand[p - pos_lo] : b.cand[p];
+    const int bins = __float_as_int(qr.w);
+    const int li = bins & 0x7ff, eb = (bins >> 11) & 0x3f, pb = bins >> 17;
     int lo, hi;
     layer_window(li, sib, P.n_layers, kDensity ? 0 : 1, &lo, &hi);
     const bool inside = staged && lo * kEtaBins >= row_lo && hi * kEtaBins + kEtaBins <= row_hi;
-    const float phi_i = b.phi[gi], zi = b.z[gi];
-    const int eb = eta_bin(b.eta[gi], P), pb = phi_bin(phi_i, P);
-    const float r0 = __fmul_rn(b.roa[gi], zi);
+    const float phi_i = cr.y, zi = qr.x, r0 = qr.y;
+    const int64_t gi = es + b.sorted[p];
     if (kDensity) {
-      const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
+      const float thr = qr.z;
       const float rho = inside ? density_of(sv, P, li, eb, pb, phi_i, zi, r0, thr, p - pos_lo)
                                : density_of(gv, P, li, eb, pb, phi_i, zi, r0, thr, p);
       b.rho[gi] = rho;
       reinterpret_cast<float*>(b.cand)[4 * (int64_t)p + 3] = rho;
     } else {
-      const float rho_i = b.rho[gi];
+      const float rho_i = cr.w;
       Nh3 o = inside ? nearest_higher_of(sv, P, li, eb, pb, phi_i, zi, r0, rho_i)
                      : nearest_higher_of(gv, P, li, eb, pb, phi_i, zi, r0, rho_i);
       if (o.nq >= 0 && inside) o.nq += pos_lo;
@@ -536,7 +562,7 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   }
   {
     NvtxRange r("clue3d/row_sort");
-    k3_row_sort<<<grid, T, 0, s>>>(b);
+    k3_row_sort<<<grid, T, 0, s>>>(b, p);
   }
   const int n_slabs = (p.n_layers + kSlabLayers - 1) / kSlabLayers;
   const int64_t slab_blocks = (int64_t)b.n_events * n_slabs;

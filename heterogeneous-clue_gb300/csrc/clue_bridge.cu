@@ -81,13 +81,22 @@ constexpr int kBridgePer = 8;
 constexpr int kBridgeRounds = kBridgeChunk / (kBridgeThreads * kBridgePer);
 static_assert(kBridgeRounds * kBridgeThreads * kBridgePer == kBridgeChunk, "chunk layout");
 
+// Seeds per event: each block counts its chunk's seeds per event in shared
+// memory (a chunk touches few events) and adds each count once; seeds of
+// events beyond the first kBlockEvents of the chunk go to global memory.
+constexpr int kBlockEvents = 32;
+
 __global__ void __launch_bounds__(kBridgeThreads) k_bridge_count(int64_t N, const int64_t* __restrict__ off,
                                                                    const int32_t* __restrict__ chunk_ev,
                                                                    const int32_t* __restrict__ seed,
                                                                    int32_t* __restrict__ counts) {
+  __shared__ int32_t s_cnt[kBlockEvents];
+  if (threadIdx.x < kBlockEvents) s_cnt[threadIdx.x] = 0;
   const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
-  int32_t e = chunk_ev[blockIdx.x];
+  const int32_t e0 = chunk_ev[blockIdx.x];
+  int32_t e = e0;
   int64_t next = off[e + 1];  // first point after event e
+  __syncthreads();
   for (int rd = 0; rd < kBridgeRounds; ++rd) {
     const int64_t i0 = c0 + (int64_t)rd * kBridgeThreads * kBridgePer + threadIdx.x;
     int32_t sv[kBridgePer];
@@ -99,107 +108,104 @@ __global__ void __launch_bounds__(kBridgeThreads) k_bridge_count(int64_t N, cons
 #pragma unroll
     for (int j = 0; j < kBridgePer; ++j) {
       const int64_t i = i0 + (int64_t)j * kBridgeThreads;
-      int32_t key = -1;
-      if (i < N) {
+      if (i < N && sv[j]) {
         while (next <= i) next = off[++e + 1];  // i grows with (rd, j)
-        if (sv[j]) key = e;
-      }
-      // one increment per event among the warp's seeds
-      const unsigned any = __ballot_sync(0xffffffffu, key >= 0);
-      if (any) {
-        const int k0 = __shfl_sync(0xffffffffu, key, __ffs(any) - 1);
-        if (__all_sync(0xffffffffu, key < 0 || key == k0)) {
-          if ((threadIdx.x & 31) == __ffs(any) - 1) atomicAdd(&counts[k0], __popc(any));
-        } else {
-          const unsigned grp = __match_any_sync(0xffffffffu, key);
-          if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[key], __popc(grp));
-        }
+        if (e - e0 < kBlockEvents) atomicAdd(&s_cnt[e - e0], 1);
+        else atomicAdd(&counts[e], 1);
       }
     }
   }
-}
-
-// Sum of a 64-bit value over the lanes of `grp` (lanes holding the same
-// cluster), exact modulo 2^64: three 22-bit limbs, each summed with one
-// 32-bit reduction (32 lanes x 2^22 < 2^32), then put back together.
-__device__ __forceinline__ unsigned long long group_sum(unsigned grp, unsigned long long v) {
-  const unsigned l0 = __reduce_add_sync(grp, (unsigned)(v & 0x3fffffu));
-  const unsigned l1 = __reduce_add_sync(grp, (unsigned)((v >> 22) & 0x3fffffu));
-  const unsigned l2 = __reduce_add_sync(grp, (unsigned)(v >> 44));
-  return (unsigned long long)l0 + ((unsigned long long)l1 << 22) + ((unsigned long long)l2 << 44);
+  __syncthreads();
+  if (threadIdx.x < kBlockEvents && s_cnt[threadIdx.x]) atomicAdd(&counts[e0 + threadIdx.x], s_cnt[threadIdx.x]);
 }
 
 // The sums of a cluster are exact integers, so they may be added in any
-// grouping: the lanes of a warp holding the same cluster add theirs first and
-// one of them makes the three atomic additions.
+// grouping: each thread takes kRun consecutive points (read 4 at a time with
+// 16-byte loads), keeps running sums while the cluster stays the same (a
+// cluster's points are mostly consecutive), and makes the three atomic
+// additions once per run.
+constexpr int kRun = kBridgeChunk / kBridgeThreads;  // 16 points per thread
+static_assert(kRun % 4 == 0, "vector loads");
+
 __global__ void __launch_bounds__(kBridgeThreads) k_bridge_accumulate(
     int64_t N, const int64_t* __restrict__ off, const int32_t* __restrict__ chunk_ev,
     const int64_t* __restrict__ coff, const float* __restrict__ x, const float* __restrict__ y,
     const float* __restrict__ w, const int32_t* __restrict__ seed, const int32_t* __restrict__ ci,
     unsigned long long* __restrict__ acc, int32_t* __restrict__ seed_of, int32_t* __restrict__ flags) {
-  const int64_t c0 = (int64_t)blockIdx.x * kBridgeChunk;
+  const int64_t i0 = (int64_t)blockIdx.x * kBridgeChunk + (int64_t)threadIdx.x * kRun;
+  if (i0 >= N) return;
   int32_t e = chunk_ev[blockIdx.x];
   int64_t next = off[e + 1];  // first point after event e
+  while (next <= i0) next = off[++e + 1];
   int64_t cbase = coff[e], ccount = coff[e + 1] - cbase;
-  const int lane = threadIdx.x & 31;
-  for (int rd = 0; rd < kBridgeRounds; ++rd) {
-    const int64_t i0 = c0 + (int64_t)rd * kBridgeThreads * kBridgePer + threadIdx.x;
-    int32_t cv[kBridgePer], sv[kBridgePer];
-    float wv[kBridgePer], xv[kBridgePer], yv[kBridgePer];
-#pragma unroll
-    for (int j = 0; j < kBridgePer; ++j) {
-      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
-      cv[j] = i < N ? ci[i] : -1;
+  int32_t cur = -1;
+  unsigned long long s0 = 0, s1 = 0, s2 = 0;
+  auto flush = [&]() {
+    if (cur >= 0) {
+      atomicAdd(&acc[3 * (int64_t)cur], s0);
+      atomicAdd(&acc[3 * (int64_t)cur + 1], s1);
+      atomicAdd(&acc[3 * (int64_t)cur + 2], s2);
     }
+  };
+  // 16-byte loads when the run is whole and every array is 16-byte aligned
+  // (i0 is a multiple of 16 points); otherwise points are read one by one
+  const bool vec = i0 + kRun <= N && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y) |
+                                      reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(seed) |
+                                      reinterpret_cast<uintptr_t>(ci)) & 15) == 0;
+  for (int k0 = 0; k0 < kRun; k0 += 4) {
+    int32_t cv[4], sv[4];
+    float wv[4], xv[4], yv[4];
+    if (vec) {
+      const int4 c4 = *reinterpret_cast<const int4*>(ci + i0 + k0);
+      const int4 s4 = *reinterpret_cast<const int4*>(seed + i0 + k0);
+      const float4 w4 = *reinterpret_cast<const float4*>(w + i0 + k0);
+      const float4 x4 = *reinterpret_cast<const float4*>(x + i0 + k0);
+      const float4 y4 = *reinterpret_cast<const float4*>(y + i0 + k0);
+      cv[0] = c4.x; cv[1] = c4.y; cv[2] = c4.z; cv[3] = c4.w;
+      sv[0] = s4.x; sv[1] = s4.y; sv[2] = s4.z; sv[3] = s4.w;
+      wv[0] = w4.x; wv[1] = w4.y; wv[2] = w4.z; wv[3] = w4.w;
+      xv[0] = x4.x; xv[1] = x4.y; xv[2] = x4.z; xv[3] = x4.w;
+      yv[0] = y4.x; yv[1] = y4.y; yv[2] = y4.z; yv[3] = y4.w;
+    } else {
 #pragma unroll
-    for (int j = 0; j < kBridgePer; ++j) {
-      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
-      const bool in = cv[j] >= 0;
-      wv[j] = in ? w[i] : 0.f;
-      xv[j] = in ? x[i] : 0.f;
-      yv[j] = in ? y[i] : 0.f;
-      sv[j] = in ? seed[i] : 0;
-    }
-#pragma unroll
-    for (int j = 0; j < kBridgePer; ++j) {
-      const int64_t i = i0 + (int64_t)j * kBridgeThreads;
-      int32_t g = -1;
-      unsigned long long v0 = 0, v1 = 0, v2 = 0;
-      if (i < N) {
-        if (next <= i) {  // i grows with (rd, j)
-          while (next <= i) next = off[++e + 1];
-          cbase = coff[e];
-          ccount = coff[e + 1] - cbase;
-        }
-        const int32_t c = cv[j];
-        if (c >= 0) {
-          if (c >= ccount) {
-            atomicExch(&flags[kFlagError], 1);
-          } else {
-            g = (int32_t)(cbase + c);
-            v0 = fx_weight(wv[j]);
-            v1 = fx_pos(wv[j], xv[j]);
-            v2 = fx_pos(wv[j], yv[j]);
-            if (sv[j]) seed_of[g] = (int32_t)i;
-          }
-        }
+      for (int j = 0; j < 4; ++j) {
+        const int64_t i = i0 + k0 + j;
+        const bool in = i < N;
+        cv[j] = in ? ci[i] : -1;
+        sv[j] = in ? seed[i] : 0;
+        wv[j] = in ? w[i] : 0.f;
+        xv[j] = in ? x[i] : 0.f;
+        yv[j] = in ? y[i] : 0.f;
       }
-      // a warp whose lanes all hold one cluster (the usual case) reduces with
-      // the full mask; otherwise the lanes are grouped by cluster first
-      const int32_t g0 = __shfl_sync(0xffffffffu, g, 0);
-      const unsigned grp = __all_sync(0xffffffffu, g == g0) ? 0xffffffffu : __match_any_sync(0xffffffffu, g);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t i = i0 + k0 + j;
+      if (i >= N) break;
+      if (next <= i) {
+        while (next <= i) next = off[++e + 1];
+        cbase = coff[e];
+        ccount = coff[e + 1] - cbase;
+      }
+      int32_t g = -1;
+      if (cv[j] >= 0) {
+        if (cv[j] >= ccount) atomicExch(&flags[kFlagError], 1);
+        else g = (int32_t)(cbase + cv[j]);
+      }
+      if (g != cur) {
+        flush();
+        cur = g;
+        s0 = s1 = s2 = 0;
+      }
       if (g >= 0) {
-        v0 = group_sum(grp, v0);
-        v1 = group_sum(grp, v1);
-        v2 = group_sum(grp, v2);
-        if (lane == __ffs(grp) - 1) {
-          atomicAdd(&acc[3 * (int64_t)g], v0);
-          atomicAdd(&acc[3 * (int64_t)g + 1], v1);
-          atomicAdd(&acc[3 * (int64_t)g + 2], v2);
-        }
+        s0 += fx_weight(wv[j]);
+        s1 += fx_pos(wv[j], xv[j]);
+        s2 += fx_pos(wv[j], yv[j]);
+        if (sv[j]) seed_of[g] = (int32_t)i;
       }
     }
   }
+  flush();
 }
 
 __global__ void k_bridge_finalize(int64_t C, const unsigned long long* __restrict__ acc,

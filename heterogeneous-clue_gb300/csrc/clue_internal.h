@@ -172,6 +172,7 @@ struct Batch3D {
   int32_t* sorted = nullptr;   // [N] event-local index, by (row, phi bin, index)
   int32_t* scol = nullptr;     // [N] phi bin of sorted entries
   float4* cand = nullptr;      // [N] by sorted position: {roa, phi, energy, rho} of the entry
+  float4* qrec = nullptr;      // [N] by sorted position: {z, roa * z, density threshold, layer | etaBin << 11 | phiBin << 17}
   int32_t* tmp = nullptr;      // [N]
   int32_t* par = nullptr;      // [N]
   int32_t* ev_seeds = nullptr; // [E] tracksters per event
