@@ -305,6 +305,29 @@ __device__ __forceinline__ void visit_row_masked(const V& v, int r, const ColMas
   for (int q = s; q < s + n1; ++q) f(q);
 }
 
+// Rows of a query's window that hold an entry in its phi columns, as bits
+// (cl - lo) * 8 + (ie - e0) of a 64-bit word: ascending bit order is the
+// reference's visiting order (layers outer, eta rows inner).  Reading every
+// row's mask in one uniform pass and then visiting only the rows whose bit is
+// set keeps the lanes of a warp together: otherwise each of the ~25 rows would
+// send the few lanes with an entry down the visit while the others wait.
+// Windows of more than 8 layers return false (the caller loops directly).
+template <class V>
+__device__ __forceinline__ bool live_rows(const V& v, int lo, int hi, int skip, int e0, int e1, const ColMask& wm,
+                                          unsigned long long* live) {
+  if (hi - lo >= 8) return false;
+  unsigned long long m = 0;
+  for (int cl = lo; cl <= hi; ++cl) {
+    if (cl == skip) continue;
+    for (int ie = e0; ie <= e1; ++ie) {
+      const int r = cl * kEtaBins + ie;
+      if ((v.m0(r) & wm.w0) | (v.m1(r) & wm.w1)) m |= 1ull << ((cl - lo) * 8 + (ie - e0));
+    }
+  }
+  *live = m;
+  return true;
+}
+
 // One cluster's density (KernelCalculateDensitySoA, :26-150) over the rows
 // in `v`; self is the cluster's own position there.
 template <class V>
@@ -313,22 +336,31 @@ __device__ __forceinline__ float density_of(const V& v, const Params3D& P, int l
   int lo, hi;
   layer_window(li, P.dens_sib, P.n_layers, 0, &lo, &hi);
   const ColMask wm(pb, 2);
+  const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
   float rho = 0.f;
-  for (int cl = lo; cl <= hi; ++cl) {
+  auto row = [&](int cl, int ie) {
     const bool same = (cl == li);
     const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
-    const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
-    for (int ie = e0; ie <= e1; ++ie) {
-      visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 2, pb + 2, [&](int q) {
-        const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
-        const float r1 = __fmul_rn(cj.x, zi);
-        const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
-        const float d0 = __fsub_rn(r0, r1);
-        const float a = __fmul_rn(d0, d0);
-        const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
-        if (__fadd_rn(a, c) < thr) rho = __fadd_rn(rho, __fmul_rn((q == self) ? 1.f : coef, cj.z));
-      });
+    visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 2, pb + 2, [&](int q) {
+      const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
+      const float r1 = __fmul_rn(cj.x, zi);
+      const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
+      const float d0 = __fsub_rn(r0, r1);
+      const float a = __fmul_rn(d0, d0);
+      const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
+      if (__fadd_rn(a, c) < thr) rho = __fadd_rn(rho, __fmul_rn((q == self) ? 1.f : coef, cj.z));
+    });
+  };
+  unsigned long long live;
+  if (live_rows(v, lo, hi, -1, e0, e1, wm, &live)) {
+    while (live) {
+      const int k = __ffsll((long long)live) - 1;
+      live &= live - 1;
+      row(lo + (k >> 3), e0 + (k & 7));
     }
+  } else {
+    for (int cl = lo; cl <= hi; ++cl)
+      for (int ie = e0; ie <= e1; ++ie) row(cl, ie);
   }
   return rho;
 }
@@ -347,25 +379,36 @@ __device__ __forceinline__ Nh3 nearest_higher_of(const V& v, const Params3D& P, 
   int lo, hi;
   layer_window(li, P.nh_sib, P.n_layers, 1, &lo, &hi);
   const ColMask wm(pb, 1);
+  const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
+  const int skip = P.nh_same ? -1 : li;
   Nh3 o;
-  for (int cl = lo; cl <= hi; ++cl) {
-    if (!P.nh_same && cl == li) continue;
-    const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
-    for (int ie = e0; ie <= e1; ++ie) {
-      visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 1, pb + 1, [&](int q) {
-        const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
-        const float r1 = __fmul_rn(cj.x, zi);
-        const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
-        const float d0 = __fsub_rn(r0, r1);
-        const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
-        if (cj.w > rho_i && d <= o.best) {  // "<=": the last candidate wins a tie
-          o.best = d;
-          o.best_t = __fsqrt_rn(d);
-          o.best_l = abs(cl - li);
-          o.nl = cl;
-          o.nq = q;
-        }
-      });
+  auto row = [&](int cl, int ie) {
+    visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 1, pb + 1, [&](int q) {
+      const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
+      const float r1 = __fmul_rn(cj.x, zi);
+      const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
+      const float d0 = __fsub_rn(r0, r1);
+      const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
+      if (cj.w > rho_i && d <= o.best) {  // "<=": the last candidate wins a tie
+        o.best = d;
+        o.best_t = __fsqrt_rn(d);
+        o.best_l = abs(cl - li);
+        o.nl = cl;
+        o.nq = q;
+      }
+    });
+  };
+  unsigned long long live;
+  if (live_rows(v, lo, hi, skip, e0, e1, wm, &live)) {
+    while (live) {
+      const int k = __ffsll((long long)live) - 1;
+      live &= live - 1;
+      row(lo + (k >> 3), e0 + (k & 7));
+    }
+  } else {
+    for (int cl = lo; cl <= hi; ++cl) {
+      if (cl == skip) continue;
+      for (int ie = e0; ie <= e1; ++ie) row(cl, ie);
     }
   }
   return o;

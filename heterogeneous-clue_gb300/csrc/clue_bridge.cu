@@ -39,12 +39,28 @@ constexpr int kBridgeThreads = 256;
 
 int chunks_for(int64_t n) { return (int)((n + kBridgeChunk - 1) / kBridgeChunk); }
 
-// Fixed-point weight, round(w * 2^24) as the double formula gives it: the
-// float product is exact (a power-of-two scale) below 2^100, and converts with
-// the same rounding; NaN, infinities and huge weights take the double formula.
+// Round-to-nearest-even of m * 2^sh for m < 2^48 and sh <= 14 (fits 63 bits).
+__device__ __forceinline__ unsigned long long round_shift(unsigned long long m, int sh) {
+  if (sh >= 0) return m << sh;
+  if (-sh > 49) return 0;  // below one half
+  const int sr = -sh;
+  const unsigned long long q = m >> sr, rem = m & ((1ull << sr) - 1), half = 1ull << (sr - 1);
+  return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
+// Fixed-point weight, round(w * 2^24) as the double formula gives it: on the
+// integer significand (the product w * 2^24 is exact), without FP64 or a
+// float-to-int64 conversion; NaN, infinities and huge weights take the
+// double formula.
 __device__ __forceinline__ unsigned long long fx_weight(float w) {
-  if (fabsf(w) < 1.2676506e30f) return (unsigned long long)__float2ll_rn(w * 16777216.f);
-  return (unsigned long long)__double2ll_rn((double)w * kWScale);
+  const unsigned uw = __float_as_uint(w);
+  int ew = (uw >> 23) & 0xff;
+  unsigned long long mw = uw & 0x7fffffu;
+  const int sh = (ew ? ew : 1) - 150 + 24;  // value = mw * 2^sh
+  if (ew == 0xff || sh > 30) return (unsigned long long)__double2ll_rn((double)w * kWScale);
+  if (ew) mw |= 0x800000u;
+  const unsigned long long q = round_shift(mw, sh);
+  return (uw >> 31) ? (0ull - q) : q;
 }
 
 // Fixed-point weighted coordinate, round(w * v * 2^16) to nearest even, as
@@ -62,17 +78,7 @@ __device__ __forceinline__ unsigned long long fx_pos(float w, float v) {
   const unsigned long long m = mw * mv;          // below 2^48
   const int sh = (ew - 150) + (ev - 150) + 16;   // value = m * 2^sh
   if (sh > 14) return (unsigned long long)__double2ll_rn((double)w * (double)v * kPScale);
-  unsigned long long q;
-  if (sh >= 0) {
-    q = m << sh;
-  } else if (-sh > 49) {
-    q = 0;  // below one half
-  } else {
-    const int sr = -sh;
-    q = m >> sr;
-    const unsigned long long rem = m & ((1ull << sr) - 1), half = 1ull << (sr - 1);
-    if (rem > half || (rem == half && (q & 1))) ++q;
-  }
+  const unsigned long long q = round_shift(m, sh);
   return ((uw ^ uv) >> 31) ? (0ull - q) : q;
 }
 
