@@ -188,7 +188,11 @@ __global__ void k3_row_sort(Batch3D b, Params3D P) {
   if (k >= 0) {
     const float zi = b.z[gi];
     const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
-    const int bins = b.layer[gi] | (eta_bin(b.eta[gi], P) << 11) | (phi_bin(b.phi[gi], P) << 17);
+    // the phi bin from the key (key = layer * 4284 + phiBin + 126 * etaBin,
+    // phiBin up to 126), without k3_key's double-precision product again
+    const int li = b.layer[gi], eb = eta_bin(b.eta[gi], P);
+    const int pbin = k - li * kBins - eb * kPhiBins;
+    const int bins = li | (eb << 11) | (pbin << 17);
     b.qrec[s + rank] = make_float4(zi, __fmul_rn(b.roa[gi], zi), thr, __int_as_float(bins));
   }
   // occupancy of the row's phi columns; bit 127 marks a column held twice
@@ -207,6 +211,7 @@ struct RowsGlobal {
   const int32_t* scol;
   __device__ __forceinline__ unsigned long long m0(int r) const { return mask[2 * r]; }
   __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * r + 1]; }
+  __device__ __forceinline__ ulonglong2 mm(int r) const { return reinterpret_cast<const ulonglong2*>(mask)[r]; }
   __device__ __forceinline__ int start(int r) const { return rstart[r]; }
   __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
   __device__ __forceinline__ int col(int q) const { return scol[q]; }
@@ -220,6 +225,9 @@ struct RowsStaged {
   int row_lo;  // first staged row
   __device__ __forceinline__ unsigned long long m0(int r) const { return mask[2 * (r - row_lo)]; }
   __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * (r - row_lo) + 1]; }
+  __device__ __forceinline__ ulonglong2 mm(int r) const {
+    return reinterpret_cast<const ulonglong2*>(mask)[r - row_lo];
+  }
   __device__ __forceinline__ int start(int r) const { return rstart[r - row_lo]; }
   __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
   __device__ __forceinline__ int col(int q) const { return scol[q]; }
@@ -320,8 +328,8 @@ __device__ __forceinline__ bool live_rows(const V& v, int lo, int hi, int skip, 
   for (int cl = lo; cl <= hi; ++cl) {
     if (cl == skip) continue;
     for (int ie = e0; ie <= e1; ++ie) {
-      const int r = cl * kEtaBins + ie;
-      if ((v.m0(r) & wm.w0) | (v.m1(r) & wm.w1)) m |= 1ull << ((cl - lo) * 8 + (ie - e0));
+      const ulonglong2 rm = v.mm(cl * kEtaBins + ie);
+      if ((rm.x & wm.w0) | (rm.y & wm.w1)) m |= 1ull << ((cl - lo) * 8 + (ie - e0));
     }
   }
   *live = m;
