@@ -296,6 +296,64 @@ def serving_leg(C, b, rate, n_req, batched=True):
             "budget_bytes": 16 << 30, "max_inflight": 2 if batched else 1}
 
 
+PIPE_POINTS = 8 << 20  # sub-batch size of the library's pipelined host-memory path
+
+
+def copy_floor(torch, off, hin, hout, dev_in, reps=3):
+    """The e2e step's copies alone, with no kernels: the same arrays in the
+    same event-aligned sub-batches of about PIPE_POINTS points as the
+    pipelined path (inputs on one stream, outputs on another, overlapped), and
+    the same bytes as one copy per array.  The pipelined e2e step cannot beat
+    the first; the host link's shared bandwidth sets both."""
+    E = len(off) - 1
+    cut = [0]
+    for e in range(E):
+        if off[e + 1] - off[cut[-1]] >= PIPE_POINTS and e + 1 < E:
+            cut.append(e + 1)
+    cut.append(E)
+    dev_out = {k: torch.empty(v.numel(), dtype=v.dtype, device="cuda") for k, v in hout.items()}
+    si, so = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def chunked():
+        with torch.cuda.stream(si):
+            for i in range(len(cut) - 1):
+                p0, p1 = int(off[cut[i]]), int(off[cut[i + 1]])
+                for k, v in hin.items():
+                    dev_in[k][p0:p1].copy_(v[p0:p1], non_blocking=True)
+        with torch.cuda.stream(so):
+            for i in range(len(cut) - 1):
+                p0, p1 = int(off[cut[i]]), int(off[cut[i + 1]])
+                for k, v in hout.items():
+                    v[p0:p1].copy_(dev_out[k][p0:p1], non_blocking=True)
+
+    def whole():
+        with torch.cuda.stream(si):
+            for k, v in hin.items():
+                dev_in[k].copy_(v, non_blocking=True)
+        with torch.cuda.stream(so):
+            for k, v in hout.items():
+                v.copy_(dev_out[k], non_blocking=True)
+
+    res = {}
+    for name, f in (("sub_batches", chunked), ("whole_arrays", whole)):
+        ts = []
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            f()
+            torch.cuda.synchronize()
+            if r:
+                ts.append(1000 * (time.perf_counter() - t0))
+        res[name + "_ms"] = statistics.median(ts)
+    nbytes = sum(v.numel() * v.element_size() for v in list(hin.values()) + list(hout.values()))
+    res["bytes"] = nbytes
+    res["sub_batches"] = len(cut) - 1
+    res["sub_batches_gb_per_s"] = nbytes / res["sub_batches_ms"] / 1e6
+    res["whole_arrays_gb_per_s"] = nbytes / res["whole_arrays_ms"] / 1e6
+    del dev_out
+    return res
+
+
 def config2_leg(C, torch, stream, args):
     """HGCAL-occupancy events (100 layers x 50 blobs of 30-80 points + 500
     noise points per layer, about 325k points each, seeds 1000 + e): the
@@ -588,6 +646,8 @@ def run_gb300(args):
                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps,
                "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)]}
+        # the same copies without the kernels, right after the timed steps
+        e2e["copy_floor"] = copy_floor(torch, off, hin, hout, dev)
         del hin, hout
 
     # the legs below use handles of their own: release the main one's buffers

@@ -12,9 +12,10 @@
 // arcs in the reference's order.
 //
 // Stages (one launch each, flattened over all events of the batch):
-//   k3_key        flat key per cluster; clusters per (event, row)
+//   k3_key        flat key per cluster; clusters per (event, row) and each
+//                 cluster's arrival slot in its row
 //   k3_row_scan   per event: first position of each row
-//   k3_scatter    place clusters into their rows (arbitrary order)
+//   k3_scatter    place clusters into their rows (arrival order)
 //   k3_row_sort   order each row by (phi bin, index)
 //   k3_search<true>   KernelCalculateDensitySoA (:26-150), one block per
 //                     (event, slab of layers) with the slab's rows staged
@@ -110,7 +111,11 @@ __global__ void k3_key(Batch3D b, Params3D P) {
   }
   const int gkey = row >= 0 ? e * b.n_rows + row : -1;
   const unsigned mask = __match_any_sync(0xffffffffu, gkey);
-  if (gkey >= 0 && (threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&b.row_cnt[gkey], __popc(mask));
+  const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+  int old = 0;
+  if (gkey >= 0 && lane == leader) old = atomicAdd(&b.row_cnt[gkey], __popc(mask));
+  old = __shfl_sync(0xffffffffu, old, leader);
+  if (gkey >= 0) b.arr[i] = old + __popc(mask & ((1u << lane) - 1u));
 }
 
 // One block per event: exclusive scan of its rows.
@@ -136,39 +141,33 @@ __global__ void __launch_bounds__(256) k3_row_scan(Batch3D b) {
   int run = (int)b.offsets[e] + before + x - sum;
   for (int r = beg; r < end; ++r) {
     b.row_start[(int64_t)e * R + r] = run;
-    b.cursor[(int64_t)e * R + r] = run;
     run += cnt[r];
   }
   if (e == b.n_events - 1 && threadIdx.x == 255) b.row_start[(int64_t)b.n_events * R] = (int)b.offsets[b.n_events];
 }
 
+// Each cluster to its arrival slot in its row: event-local index and phi
+// column, the input of the rank below.
 __global__ void k3_scatter(Batch3D b) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int gkey = -1, e = 0, k = -1;
-  if (i < b.n_points) {
-    e = event_of(b.offsets, b.n_events, i);
-    k = b.key[i];
-    gkey = e * b.n_rows + row_of(k, b.n_rows);
-  }
-  const unsigned mask = __match_any_sync(0xffffffffu, gkey);
-  const int leader = __ffs(mask) - 1;
-  const int lane = threadIdx.x & 31;
-  int pos = 0;
-  if (gkey >= 0 && lane == leader) pos = atomicAdd(&b.cursor[gkey], __popc(mask));
-  pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(mask & ((1u << lane) - 1u));
-  if (gkey >= 0) {
-    b.tmp[pos] = (int32_t)(i - b.offsets[e]);  // event-local index
-    b.par[pos] = k >= 0 ? k % kPhiBins : 0;     // phi column
-  }
+  if (i >= b.n_points) return;
+  const int e = event_of(b.offsets, b.n_events, i);
+  const int k = b.key[i];
+  const int pos = b.row_start[(int64_t)e * b.n_rows + row_of(k, b.n_rows)] + b.arr[i];
+  b.tmp[pos] = (int32_t)(i - b.offsets[e]);
+  b.par[pos] = k >= 0 ? k % kPhiBins : 0;
 }
 
 // Each entry's rank inside its row by (column, index) gives its final slot.
+// One thread per scattered entry: the threads of a row read the same few
+// entries.
 __global__ void k3_row_sort(Batch3D b, Params3D P) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= b.n_points) return;
   const int e = event_of(b.offsets, b.n_events, p);
   const int idx = b.tmp[p], col = b.par[p];
-  const int k = b.key[b.offsets[e] + idx];
+  const int64_t gi = b.offsets[e] + idx;
+  const int k = b.key[gi];
   const int64_t r = (int64_t)e * b.n_rows + row_of(k, b.n_rows);
   const int s = b.row_start[r], t = b.row_start[r + 1];
   int rank = 0;
@@ -176,13 +175,13 @@ __global__ void k3_row_sort(Batch3D b, Params3D P) {
     const int c2 = b.par[q], i2 = b.tmp[q];
     rank += (c2 < col) || (c2 == col && i2 < idx);
   }
-  b.sorted[s + rank] = idx;
-  b.scol[s + rank] = col;
+  const int f = s + rank;
+  b.sorted[f] = idx;
+  b.scol[f] = col;
   // what the searches read of a candidate, in sorted order: a run of a row's
   // entries is then one contiguous stretch of 16-byte records (rho follows
   // from the density search)
-  const int64_t gi = b.offsets[e] + idx;
-  b.cand[s + rank] = make_float4(b.roa[gi], b.phi[gi], b.energy[gi], 0.f);
+  b.cand[f] = make_float4(b.roa[gi], b.phi[gi], b.energy[gi], 0.f);
   // and what a search needs of the entry as a query, so that the searches
   // read their queries in sorted order instead of gathering them
   if (k >= 0) {
@@ -193,7 +192,7 @@ __global__ void k3_row_sort(Batch3D b, Params3D P) {
     const int li = b.layer[gi], eb = eta_bin(b.eta[gi], P);
     const int pbin = k - li * kBins - eb * kPhiBins;
     const int bins = li | (eb << 11) | (pbin << 17);
-    b.qrec[s + rank] = make_float4(zi, __fmul_rn(b.roa[gi], zi), thr, __int_as_float(bins));
+    b.qrec[f] = make_float4(zi, __fmul_rn(b.roa[gi], zi), thr, __int_as_float(bins));
   }
   // occupancy of the row's phi columns; bit 127 marks a column held twice
   unsigned long long* m = b.row_mask + 2 * r;
@@ -211,7 +210,6 @@ struct RowsGlobal {
   const int32_t* scol;
   __device__ __forceinline__ unsigned long long m0(int r) const { return mask[2 * r]; }
   __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * r + 1]; }
-  __device__ __forceinline__ ulonglong2 mm(int r) const { return reinterpret_cast<const ulonglong2*>(mask)[r]; }
   __device__ __forceinline__ int start(int r) const { return rstart[r]; }
   __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
   __device__ __forceinline__ int col(int q) const { return scol[q]; }
@@ -277,10 +275,26 @@ __device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long l
 // (the reference's iphi = iphi_it mod nPhiBins, CLUE3DAlgoKernels.h:80-84).
 struct ColMask {
   unsigned long long w0 = 0, w1 = 0;
-  __device__ __forceinline__ ColMask(int pb, int d) {
-    for (int c = pb - d; c <= pb + d; ++c) {
-      const int cc = c < 0 ? c + kPhiBins : (c >= kPhiBins ? c - kPhiBins : c);
-      if (cc < 64) w0 |= 1ull << cc; else w1 |= 1ull << (cc - 64);
+  // columns [lo, lo + n), 0 <= n <= 5, lo + n <= 126
+  __device__ __forceinline__ void run(int lo, int n) {
+    const unsigned long long r = (1ull << n) - 1;
+    if (lo >= 64) {
+      w1 |= r << (lo - 64);
+    } else {
+      w0 |= r << lo;
+      if (lo + n > 64) w1 |= r >> (64 - lo);
+    }
+  }
+  __device__ __forceinline__ ColMask(int pb, int d) {  // 0 <= pb <= 126, d <= 2
+    const int a = pb - d, c = pb + d;
+    if (a < 0) {
+      run(a + kPhiBins, -a);
+      run(0, c + 1);
+    } else if (c >= kPhiBins) {
+      run(a, kPhiBins - a);
+      run(0, c - kPhiBins + 1);
+    } else {
+      run(a, 2 * d + 1);
     }
   }
 };
@@ -336,41 +350,28 @@ __device__ __forceinline__ bool live_rows(const V& v, int lo, int hi, int skip, 
   return true;
 }
 
-// One cluster's density (KernelCalculateDensitySoA, :26-150) over the rows
-// in `v`; self is the cluster's own position there.
+// What a search needs of its query cluster.
+struct Query3 {
+  float phi, z, r0, aux;  // aux: density threshold (density), rho (nearest higher)
+  int li, eb, pb, self;   // self: the cluster's own position in the view
+};
+
+// Density terms of one row of a query's window (KernelCalculateDensitySoA,
+// :26-150): the clusters of the row in the window's phi columns, in order.
 template <class V>
-__device__ __forceinline__ float density_of(const V& v, const Params3D& P, int li, int eb, int pb, float phi_i,
-                                            float zi, float r0, float thr, int self) {
-  int lo, hi;
-  layer_window(li, P.dens_sib, P.n_layers, 0, &lo, &hi);
-  const ColMask wm(pb, 2);
-  const int e0 = max(eb - 2, 0), e1 = min(eb + 2, kEtaBins);
-  float rho = 0.f;
-  auto row = [&](int cl, int ie) {
-    const bool same = (cl == li);
-    const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
-    visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 2, pb + 2, [&](int q) {
-      const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
-      const float r1 = __fmul_rn(cj.x, zi);
-      const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
-      const float d0 = __fsub_rn(r0, r1);
-      const float a = __fmul_rn(d0, d0);
-      const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
-      if (__fadd_rn(a, c) < thr) rho = __fadd_rn(rho, __fmul_rn((q == self) ? 1.f : coef, cj.z));
-    });
-  };
-  unsigned long long live;
-  if (live_rows(v, lo, hi, -1, e0, e1, wm, &live)) {
-    while (live) {
-      const int k = __ffsll((long long)live) - 1;
-      live &= live - 1;
-      row(lo + (k >> 3), e0 + (k & 7));
-    }
-  } else {
-    for (int cl = lo; cl <= hi; ++cl)
-      for (int ie = e0; ie <= e1; ++ie) row(cl, ie);
-  }
-  return rho;
+__device__ __forceinline__ void density_row(const V& v, const Params3D& P, const Query3& Q, const ColMask& wm, int cl,
+                                            int ie, float& rho) {
+  const bool same = (cl == Q.li);
+  const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
+  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 2, Q.pb + 2, [&](int q) {
+    const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
+    const float r1 = __fmul_rn(cj.x, Q.z);
+    const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
+    const float d0 = __fsub_rn(Q.r0, r1);
+    const float a = __fmul_rn(d0, d0);
+    const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
+    if (__fadd_rn(a, c) < Q.aux) rho = __fadd_rn(rho, __fmul_rn((q == Q.self) ? 1.f : coef, cj.z));
+  });
 }
 
 // One cluster's nearest higher (KernelComputeDistanceToHigherSoA, :286-392)
@@ -382,44 +383,67 @@ struct Nh3 {
 };
 
 template <class V>
-__device__ __forceinline__ Nh3 nearest_higher_of(const V& v, const Params3D& P, int li, int eb, int pb, float phi_i,
-                                                 float zi, float r0, float rho_i) {
-  int lo, hi;
-  layer_window(li, P.nh_sib, P.n_layers, 1, &lo, &hi);
-  const ColMask wm(pb, 1);
-  const int e0 = max(eb - 1, 0), e1 = min(eb + 1, kEtaBins);
-  const int skip = P.nh_same ? -1 : li;
-  Nh3 o;
-  auto row = [&](int cl, int ie) {
-    visit_row_masked(v, cl * kEtaBins + ie, wm, pb - 1, pb + 1, [&](int q) {
-      const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
-      const float r1 = __fmul_rn(cj.x, zi);
-      const float dphi = reduce_range(__fsub_rn(phi_i, cj.y), P);
-      const float d0 = __fsub_rn(r0, r1);
-      const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
-      if (cj.w > rho_i && d <= o.best) {  // "<=": the last candidate wins a tie
-        o.best = d;
-        o.best_t = __fsqrt_rn(d);
-        o.best_l = abs(cl - li);
-        o.nl = cl;
-        o.nq = q;
-      }
-    });
-  };
-  unsigned long long live;
-  if (live_rows(v, lo, hi, skip, e0, e1, wm, &live)) {
-    while (live) {
-      const int k = __ffsll((long long)live) - 1;
-      live &= live - 1;
-      row(lo + (k >> 3), e0 + (k & 7));
+__device__ __forceinline__ void nh_row(const V& v, const Params3D& P, const Query3& Q, const ColMask& wm, int cl, int ie,
+                                       Nh3& o) {
+  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 1, Q.pb + 1, [&](int q) {
+    const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
+    const float r1 = __fmul_rn(cj.x, Q.z);
+    const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
+    const float d0 = __fsub_rn(Q.r0, r1);
+    const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
+    if (cj.w > Q.aux && d <= o.best) {  // "<=": the last candidate wins a tie
+      o.best = d;
+      o.best_t = __fsqrt_rn(d);
+      o.best_l = abs(cl - Q.li);
+      o.nl = cl;
+      o.nq = q;
     }
-  } else {
-    for (int cl = lo; cl <= hi; ++cl) {
-      if (cl == skip) continue;
-      for (int ie = e0; ie <= e1; ++ie) row(cl, ie);
+  });
+}
+
+// The window of a query: layers [lo, hi] (without `skip`), eta rows
+// [e0, e1], phi columns pb +- d.
+struct Window3 {
+  int lo, hi, e0, e1, skip;
+};
+
+__device__ __forceinline__ Window3 window_of(const Params3D& P, const Query3& Q, bool density) {
+  Window3 w;
+  const int de = density ? 2 : 1;
+  layer_window(Q.li, density ? P.dens_sib : P.nh_sib, P.n_layers, density ? 0 : 1, &w.lo, &w.hi);
+  w.e0 = max(Q.eb - de, 0);
+  w.e1 = min(Q.eb + de, kEtaBins);
+  w.skip = (density || P.nh_same) ? -1 : Q.li;
+  return w;
+}
+
+// A whole search over the rows of `v`, every window row in order (the rows
+// whose mask shows no entry return at once).
+template <bool kDensity, class V, class R>
+__device__ __forceinline__ void search_all(const V& v, const Params3D& P, const Query3& Q, R& res) {
+  const Window3 w = window_of(P, Q, kDensity);
+  const ColMask wm(Q.pb, kDensity ? 2 : 1);
+  for (int cl = w.lo; cl <= w.hi; ++cl) {
+    if (cl == w.skip) continue;
+    for (int ie = w.e0; ie <= w.e1; ++ie) {
+      if constexpr (kDensity) density_row(v, P, Q, wm, cl, ie, res);
+      else nh_row(v, P, Q, wm, cl, ie, res);
     }
   }
-  return o;
+}
+
+// The same search over the rows named by a live_rows() mask.
+template <bool kDensity, class V, class R>
+__device__ __forceinline__ void search_live(const V& v, const Params3D& P, const Query3& Q, unsigned long long live,
+                                            R& res) {
+  const Window3 w = window_of(P, Q, kDensity);
+  const ColMask wm(Q.pb, kDensity ? 2 : 1);
+  while (live) {
+    const int k = __ffsll((long long)live) - 1;
+    live &= live - 1;
+    if constexpr (kDensity) density_row(v, P, Q, wm, w.lo + (k >> 3), w.e0 + (k & 7), res);
+    else nh_row(v, P, Q, wm, w.lo + (k >> 3), w.e0 + (k & 7), res);
+  }
 }
 
 // Staging of the searches: one block per (event, slab of kSlabLayers
@@ -474,28 +498,50 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
   RowsStaged sv{s_mask, s_rs, s_cand, s_col, row_lo};
   RowsGlobal gv{b.row_mask + 2 * rbase, rs, b.cand, b.scol};
   const int64_t es = b.offsets[e];
-  for (int p = q_lo + (int)threadIdx.x; p < q_hi; p += kSlabThreads) {
-    // the query rows hold only accepted clusters (rejected ones are in the
-    // event's last row); a query's own data is read in sorted order
+  const int tid = threadIdx.x;
+  // the query rows hold only accepted clusters (rejected ones are in the
+  // event's last row); a query's own data is read in sorted order
+  auto query = [&](int p, bool* inside) {
     const float4 qr = b.qrec[p];
     const float4 cr = staged ? s_cand[p - pos_lo] : b.cand[p];
     const int bins = __float_as_int(qr.w);
-    const int li = bins & 0x7ff, eb = (bins >> 11) & 0x3f, pb = bins >> 17;
+    Query3 Q;
+    Q.li = bins & 0x7ff;
+    Q.eb = (bins >> 11) & 0x3f;
+    Q.pb = bins >> 17;
+    Q.phi = cr.y;
+    Q.z = qr.x;
+    Q.r0 = qr.y;
+    Q.aux = kDensity ? qr.z : cr.w;
     int lo, hi;
-    layer_window(li, sib, P.n_layers, kDensity ? 0 : 1, &lo, &hi);
-    const bool inside = staged && lo * kEtaBins >= row_lo && hi * kEtaBins + kEtaBins <= row_hi;
-    const float phi_i = cr.y, zi = qr.x, r0 = qr.y;
+    layer_window(Q.li, sib, P.n_layers, kDensity ? 0 : 1, &lo, &hi);
+    *inside = staged && lo * kEtaBins >= row_lo && hi * kEtaBins + kEtaBins <= row_hi;
+    Q.self = *inside ? p - pos_lo : p;
+    return Q;
+  };
+  for (int p = q_lo + tid; p < q_hi; p += kSlabThreads) {
+    bool inside;
+    const Query3 Q = query(p, &inside);
     const int64_t gi = es + b.sorted[p];
-    if (kDensity) {
-      const float thr = qr.z;
-      const float rho = inside ? density_of(sv, P, li, eb, pb, phi_i, zi, r0, thr, p - pos_lo)
-                               : density_of(gv, P, li, eb, pb, phi_i, zi, r0, thr, p);
+    // staged windows: the rows holding an entry first, in one uniform pass
+    unsigned long long live = 0;
+    bool by_live = false;
+    if (inside) {
+      const Window3 w = window_of(P, Q, kDensity);
+      by_live = live_rows(sv, w.lo, w.hi, w.skip, w.e0, w.e1, ColMask(Q.pb, kDensity ? 2 : 1), &live);
+    }
+    if constexpr (kDensity) {
+      float rho = 0.f;
+      if (by_live) search_live<true>(sv, P, Q, live, rho);
+      else if (inside) search_all<true>(sv, P, Q, rho);
+      else search_all<true>(gv, P, Q, rho);
       b.rho[gi] = rho;
       reinterpret_cast<float*>(b.cand)[4 * (int64_t)p + 3] = rho;
     } else {
-      const float rho_i = cr.w;
-      Nh3 o = inside ? nearest_higher_of(sv, P, li, eb, pb, phi_i, zi, r0, rho_i)
-                     : nearest_higher_of(gv, P, li, eb, pb, phi_i, zi, r0, rho_i);
+      Nh3 o;
+      if (by_live) search_live<false>(sv, P, Q, live, o);
+      else if (inside) search_all<false>(sv, P, Q, o);
+      else search_all<false>(gv, P, Q, o);
       if (o.nq >= 0 && inside) o.nq += pos_lo;
       if (o.best != FLT_MAX) {
         b.delta_t[gi] = o.best_t;

@@ -45,7 +45,7 @@ Params3D make_params3d(const clue3d_params& q) {
 }
 
 enum Slot3D : int {
-  T_OFF, T_KEY, T_RCNT, T_RSTART, T_CURSOR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_CAND, T_QREC,
+  T_OFF, T_KEY, T_RCNT, T_RSTART, T_ARR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_CAND, T_QREC,
   T_IN0, T_IN1, T_IN2, T_IN3, T_IN4, T_IN5, T_IN6, T_IN7,
   T_OUT0, T_OUT1, T_OUT2, T_OUT3, T_OUT4, T_OUT5, T_OUT6,
   T_COUNT
@@ -111,8 +111,8 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     const bool host_io = !(flags & CLUE_DEVICE_MEMORY);
     std::vector<size_t> need(T_COUNT, 0);
     need[T_OFF] = 8 * (size_t)(E + 1);
-    need[T_KEY] = need[T_SORTED] = need[T_SCOL] = need[T_TMP] = need[T_PAR] = 4 * (size_t)N;
-    need[T_RCNT] = need[T_CURSOR] = 4 * (size_t)(E * n_rows);
+    need[T_KEY] = need[T_ARR] = need[T_SORTED] = need[T_SCOL] = need[T_TMP] = need[T_PAR] = 4 * (size_t)N;
+    need[T_RCNT] = 4 * (size_t)(E * n_rows);
     need[T_RSTART] = 4 * (size_t)(E * n_rows + 1);
     need[T_EVSEEDS] = 4 * (size_t)E;
     need[T_FLAGS] = 4 * kFlagCount;
@@ -172,7 +172,7 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     b.key = static_cast<int32_t*>(P(T_KEY));
     b.row_cnt = static_cast<int32_t*>(P(T_RCNT));
     b.row_start = static_cast<int32_t*>(P(T_RSTART));
-    b.cursor = static_cast<int32_t*>(P(T_CURSOR));
+    b.arr = static_cast<int32_t*>(P(T_ARR));
     b.sorted = static_cast<int32_t*>(P(T_SORTED));
     b.scol = static_cast<int32_t*>(P(T_SCOL));
     b.tmp = static_cast<int32_t*>(P(T_TMP));

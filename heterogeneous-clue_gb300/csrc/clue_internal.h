@@ -168,7 +168,7 @@ struct Batch3D {
   int32_t* key = nullptr;      // [N] flat (layer, eta, phi) bin
   int32_t* row_cnt = nullptr;  // [E * n_rows + 1]
   int32_t* row_start = nullptr;// [E * n_rows + 1]
-  int32_t* cursor = nullptr;   // [E * n_rows]
+  int32_t* arr = nullptr;      // [N] arrival slot of each cluster in its row
   int32_t* sorted = nullptr;   // [N] event-local index, by (row, phi bin, index)
   int32_t* scol = nullptr;     // [N] phi bin of sorted entries
   float4* cand = nullptr;      // [N] by sorted position: {roa, phi, energy, rho} of the entry
