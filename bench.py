@@ -7,19 +7,25 @@ far larger than the 129 MB L2, so no flush is needed between steps).
 * ``value``: events/s of the batched path (one CUDA-graph replay per step),
   inputs and outputs resident in HBM, CUDA events on the launching stream.
 * ``e2e``: the same through the C ABI with host (pinned) buffers, H2D of the
-  inputs and D2H of all five outputs inside every step.
+  inputs and D2H of all five outputs inside every step; ``e2e.copy_floor``
+  times the same copies without the kernels right after, in the pipelined
+  path's sub-batches and as whole arrays (the host link's floor on this machine).
 * ``roofline``: the dominant kernel (k_layers), timed per stage with CUDA
   events on its stream in a second pass over the same workload; algorithmic
   bytes = 80 B per point (the reference's four stages each streaming their
   SoA inputs once and writing their outputs once).
 * ``plain_*``: the same kernels one event per launch sequence.
-* ``cpu_baseline``: the oracle port (a C restatement of the reference serial
-  algorithm, bit-identical to it) over all host cores on a bounded sample.
+* ``cpu_baseline``: the reference's own serial algorithm
+  (``CLUEAlgoSerial::makeClusters``, compiled from its unmodified sources by
+  ``oracle/build.py`` into ``oracle/_ref``) over all host cores on a bounded
+  sample, kind "reference"; the oracle port (a C restatement, bit-identical)
+  is timed beside it, and stands in (kind "port") where the reference's
+  sources were not available to build.
 * ``serving``: Poisson arrivals into the continuous-batching server and into
   a one-event server, at a fixed load and at a load above the latter's
   capacity; ``clue3d``: batched CLUE3D on 1,000 events of layer clusters;
   ``hgcal_1000``: batched and plain on 1,000 HGCAL-occupancy events (about
-  325k points each).
+  325k points each), and the chain 2D -> bridge -> CLUE3D on them.
 
 ``--impl reference`` times that CPU implementation alone on the same
 workload and prints the reference arm's line.
@@ -645,7 +651,8 @@ def run_gb300(args):
         e2e = {"value": ws * E * args.steps / dt, "unit": "events/s",
                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                "gpoints_per_s": ws * N * args.steps / dt / 1e9, "ms_per_step": 1000 * dt / args.steps,
-               "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)]}
+               "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
+               "step_ms": [round(t, 3) for t in step_ms]}
         # the same copies without the kernels, right after the timed steps
         e2e["copy_floor"] = copy_floor(torch, off, hin, hout, dev)
         del hin, hout

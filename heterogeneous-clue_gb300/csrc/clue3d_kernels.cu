@@ -118,6 +118,16 @@ __global__ void k3_key(Batch3D b, Params3D P) {
   if (gkey >= 0) b.arr[i] = old + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Entries of a row whose phi column lies in [a, c] (0 <= a <= c <= 125) are
+// one run of the row (entries are sorted by column): its first position and
+// length, from the column-occupancy mask, when no column repeats.
+__device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long long m1, int p) {
+  // set bits of columns < p (0 <= p <= 126)
+  if (p <= 0) return 0;
+  if (p < 64) return __popcll(m0 & ((1ull << p) - 1));
+  return __popcll(m0) + __popcll(m1 & ((1ull << (p - 64)) - 1));
+}
+
 // One block per event: exclusive scan of its rows.
 __global__ void __launch_bounds__(256) k3_row_scan(Batch3D b) {
   const int e = blockIdx.x;
@@ -146,58 +156,71 @@ __global__ void __launch_bounds__(256) k3_row_scan(Batch3D b) {
   if (e == b.n_events - 1 && threadIdx.x == 255) b.row_start[(int64_t)b.n_events * R] = (int)b.offsets[b.n_events];
 }
 
-// Each cluster to its arrival slot in its row: event-local index and phi
-// column, the input of the rank below.
-__global__ void k3_scatter(Batch3D b) {
+// Each cluster to its arrival slot in its row, with everything the row sort
+// and the searches need of it, read here in input order (coalesced): its
+// event-local index, phi column and row; its 16-byte candidate record {roa,
+// phi, energy, rho} (rho added by the density search); its 16-byte query
+// record {z, roa * z, density threshold, layer | etaBin << 11 | phiBin << 17}.
+// The cluster also goes into its row's 128-bit phi-column occupancy mask;
+// bit 127 marks a column held twice.
+__global__ void k3_scatter(Batch3D b, Params3D P) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= b.n_points) return;
   const int e = event_of(b.offsets, b.n_events, i);
   const int k = b.key[i];
-  const int pos = b.row_start[(int64_t)e * b.n_rows + row_of(k, b.n_rows)] + b.arr[i];
+  const int row = row_of(k, b.n_rows);
+  const int64_t r = (int64_t)e * b.n_rows + row;
+  const int pos = b.row_start[r] + b.arr[i];
+  const int col = k >= 0 ? k % kPhiBins : 0;
   b.tmp[pos] = (int32_t)(i - b.offsets[e]);
-  b.par[pos] = k >= 0 ? k % kPhiBins : 0;
+  b.par[pos] = col | (row << 7);
+  const float roa = b.roa[i];
+  b.tcand[pos] = make_float4(roa, b.phi[i], b.energy[i], 0.f);
+  if (k >= 0) {
+    const float zi = b.z[i];
+    const float thr = b.sil[i] ? P.dens_thr : __fmul_rn(b.radius[i], b.radius[i]);
+    // the phi bin from the key (key = layer * 4284 + phiBin + 126 * etaBin,
+    // phiBin up to 126), without k3_key's double-precision product again
+    const int li = b.layer[i], eb = eta_bin(b.eta[i], P);
+    const int pbin = k - li * kBins - eb * kPhiBins;
+    const int bins = li | (eb << 11) | (pbin << 17);
+    b.tqrec[pos] = make_float4(zi, __fmul_rn(roa, zi), thr, __int_as_float(bins));
+  }
+  unsigned long long* m = b.row_mask + 2 * r;
+  const unsigned long long bit = 1ull << (col & 63);
+  if (atomicOr(m + (col >> 6), bit) & bit) atomicOr(m + 1, 1ull << 63);
 }
 
-// Each entry's rank inside its row by (column, index) gives its final slot.
-// One thread per scattered entry: the threads of a row read the same few
-// entries.
-__global__ void k3_row_sort(Batch3D b, Params3D P) {
+// Each entry's rank inside its row by (column, index) gives its final slot:
+// a counting sort by column through the occupancy mask (the entries in lower
+// columns are the mask's set bits below the entry's column) when no column
+// repeats, a count over the row otherwise.  One thread per scattered entry;
+// its records move within the row's range.
+__global__ void k3_row_sort(Batch3D b) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= b.n_points) return;
   const int e = event_of(b.offsets, b.n_events, p);
-  const int idx = b.tmp[p], col = b.par[p];
-  const int64_t gi = b.offsets[e] + idx;
-  const int k = b.key[gi];
-  const int64_t r = (int64_t)e * b.n_rows + row_of(k, b.n_rows);
-  const int s = b.row_start[r], t = b.row_start[r + 1];
-  int rank = 0;
-  for (int q = s; q < t; ++q) {
-    const int c2 = b.par[q], i2 = b.tmp[q];
-    rank += (c2 < col) || (c2 == col && i2 < idx);
+  const int idx = b.tmp[p], cr = b.par[p];
+  const int col = cr & 127;
+  const int64_t r = (int64_t)e * b.n_rows + (cr >> 7);
+  const int s = b.row_start[r];
+  const ulonglong2 m = reinterpret_cast<const ulonglong2*>(b.row_mask)[r];
+  int rank;
+  if (!(m.y >> 63)) {
+    rank = bits_below(m.x, m.y, col);
+  } else {
+    const int t = b.row_start[r + 1];
+    rank = 0;
+    for (int q = s; q < t; ++q) {
+      const int c2 = b.par[q] & 127, i2 = b.tmp[q];
+      rank += (c2 < col) || (c2 == col && i2 < idx);
+    }
   }
   const int f = s + rank;
   b.sorted[f] = idx;
   b.scol[f] = col;
-  // what the searches read of a candidate, in sorted order: a run of a row's
-  // entries is then one contiguous stretch of 16-byte records (rho follows
-  // from the density search)
-  b.cand[f] = make_float4(b.roa[gi], b.phi[gi], b.energy[gi], 0.f);
-  // and what a search needs of the entry as a query, so that the searches
-  // read their queries in sorted order instead of gathering them
-  if (k >= 0) {
-    const float zi = b.z[gi];
-    const float thr = b.sil[gi] ? P.dens_thr : __fmul_rn(b.radius[gi], b.radius[gi]);
-    // the phi bin from the key (key = layer * 4284 + phiBin + 126 * etaBin,
-    // phiBin up to 126), without k3_key's double-precision product again
-    const int li = b.layer[gi], eb = eta_bin(b.eta[gi], P);
-    const int pbin = k - li * kBins - eb * kPhiBins;
-    const int bins = li | (eb << 11) | (pbin << 17);
-    b.qrec[f] = make_float4(zi, __fmul_rn(b.roa[gi], zi), thr, __int_as_float(bins));
-  }
-  // occupancy of the row's phi columns; bit 127 marks a column held twice
-  unsigned long long* m = b.row_mask + 2 * r;
-  const unsigned long long bit = 1ull << (col & 63);
-  if (atomicOr(m + (col >> 6), bit) & bit) atomicOr(m + 1, 1ull << 63);
+  b.cand[f] = b.tcand[p];
+  b.qrec[f] = b.tqrec[p];  // rejected clusters (the junk row) carry no query record
 }
 
 // The rows of one event as the searches see them: the whole event in global
@@ -259,16 +282,6 @@ __device__ __forceinline__ void visit_row(const V& v, int s, int t, int p0, int 
     if (c > c1) break;
     if (c >= c0) f(q);
   }
-}
-
-// Entries of a row whose phi column lies in [a, c] (0 <= a <= c <= 125) are
-// one run of the row (entries are sorted by column): its first position and
-// length, from the column-occupancy mask, when no column repeats.
-__device__ __forceinline__ int bits_below(unsigned long long m0, unsigned long long m1, int p) {
-  // set bits of columns < p (0 <= p <= 126)
-  if (p <= 0) return 0;
-  if (p < 64) return __popcll(m0 & ((1ull << p) - 1));
-  return __popcll(m0) + __popcll(m1 & ((1ull << (p - 64)) - 1));
 }
 
 // Phi columns of the window [pb - d, pb + d] modulo 126 as a 126-bit mask
@@ -655,11 +668,11 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   }
   {
     NvtxRange r("clue3d/scatter");
-    k3_scatter<<<grid, T, 0, s>>>(b);
+    k3_scatter<<<grid, T, 0, s>>>(b, p);
   }
   {
     NvtxRange r("clue3d/row_sort");
-    k3_row_sort<<<grid, T, 0, s>>>(b, p);
+    k3_row_sort<<<grid, T, 0, s>>>(b);
   }
   const int n_slabs = (p.n_layers + kSlabLayers - 1) / kSlabLayers;
   const int64_t slab_blocks = (int64_t)b.n_events * n_slabs;

@@ -173,6 +173,8 @@ struct Batch3D {
   int32_t* scol = nullptr;     // [N] phi bin of sorted entries
   float4* cand = nullptr;      // [N] by sorted position: {roa, phi, energy, rho} of the entry
   float4* qrec = nullptr;      // [N] by sorted position: {z, roa * z, density threshold, layer | etaBin << 11 | phiBin << 17}
+  float4* tcand = nullptr;     // [N] cand records by scatter position
+  float4* tqrec = nullptr;     // [N] qrec records by scatter position
   int32_t* tmp = nullptr;      // [N]
   int32_t* par = nullptr;      // [N]
   int32_t* ev_seeds = nullptr; // [E] tracksters per event

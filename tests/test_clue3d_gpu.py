@@ -127,3 +127,58 @@ def test_side_boundary_and_high_eta_3d(algo, prm):
     want, wnt = oracle.clue3d(ev, **prm)
     assert nt[0] == wnt
     assert_bitexact(_as_oracle(out), want, KEYS_3D)
+
+
+def _event3d(eta, phi, layer, seed):
+    """A CLUE3D event from given eta, phi and layer (the other fields derived
+    as the synthetic generator derives them)."""
+    rng = np.random.default_rng(seed)
+    k = eta.size
+    z = S.layer_z(100)[layer]
+    roa = (1.0 / np.sinh(eta.astype(np.float64))).astype(np.float32)
+    r = roa * z
+    phi = phi.astype(np.float32)
+    return dict(x=(r * np.cos(phi)).astype(np.float32), y=(r * np.sin(phi)).astype(np.float32),
+                z=z.astype(np.float32), eta=eta.astype(np.float32), phi=phi, r_over_absz=roa,
+                radius=np.full(k, 2.0, np.float32), layer=layer.astype(np.int32),
+                energy=np.exp(0.7 * rng.standard_normal(k)).astype(np.float32), isSilicon=np.ones(k, np.int32))
+
+
+def test_dense_rows_and_staging_overflow_3d(algo):
+    """Rows far from the typical three entries: one (layer, eta) row with an
+    entry in every phi column (the column-count rank with a full mask), one
+    column holding 60 entries (the walked rank and walked visits), and a slab
+    of four layers with 3,000 clusters, above the searches' on-chip staging
+    capacity (the global-memory path), each with a sprinkle of other clusters,
+    in shuffled order; every output against the oracle."""
+    rng = np.random.default_rng(2024)
+    bw = 2 * np.pi / 126
+    evs = []
+    # every phi column of layer 10, eta bin 2, plus neighbours in eta and layer
+    c = np.arange(126)
+    phi = (c + rng.uniform(0.1, 0.9, 126)) * bw - np.pi
+    eta = np.full(126, 1.5 + 2.5 / 20)
+    lay = np.full(126, 10)
+    eta = np.concatenate([eta, rng.uniform(1.5, 1.8, 400)])
+    phi = np.concatenate([phi, rng.uniform(-np.pi, np.pi, 400)])
+    lay = np.concatenate([lay, rng.choice([8, 9, 11, 12], 400)])  # the full row keeps one entry per column
+    evs.append((eta, phi, lay))
+    # 60 clusters in one (layer, eta, phi) bin, neighbours around it
+    eta = np.concatenate([np.full(60, 1.5 + 5.5 / 20), rng.uniform(1.7, 1.9, 300)])
+    phi = np.concatenate([(40 + rng.uniform(0.05, 0.95, 60)) * bw - np.pi, (rng.uniform(36, 45, 300)) * bw - np.pi])
+    lay = np.concatenate([np.full(60, 30), rng.integers(27, 34, 300)])
+    evs.append((eta, phi, lay))
+    # 3,000 clusters in layers 20-23 (plus siblings): above the staging capacity
+    eta = rng.uniform(1.5, 3.0, 3600)
+    phi = rng.uniform(-np.pi, np.pi, 3600)
+    lay = np.concatenate([rng.integers(20, 24, 3000), rng.integers(16, 28, 600)])
+    evs.append((eta, phi, lay))
+    events = []
+    for i, (eta, phi, lay) in enumerate(evs):
+        perm = rng.permutation(eta.size)
+        events.append(_event3d(eta[perm], phi[perm], lay[perm], 50 + i))
+    b = S.concat3d(events)
+    out, nts = algo.run_clue3d(b["offsets"], b, params=CONFIG4)
+    want, wnt = _oracle_batch(b, CONFIG4)
+    assert np.array_equal(nts, wnt)
+    assert_bitexact(_as_oracle(out), want, KEYS_3D, label="dense rows")
