@@ -49,13 +49,16 @@ BYTES_PER_POINT = 80          # algorithmic bytes per point, all four stages
 COMPULSORY_BYTES_PER_POINT = 36
 PARAMS = (1.3, 2.0, 2.0)
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
-# of the 256-event uneven batch (dram read + write over its 13.6M points);
+# of the 256-event uneven batch (dram read + write over its 13,628,373 points);
 # traffic grows with the point count, so a full launch is scaled by its points.
-K_LAYERS_DRAM_BYTES_PER_POINT = 24.77
+K_LAYERS_DRAM_BYTES_PER_POINT = 24.50
 # Warp instructions per point of k_layers (both passes), same capture: the
 # kernel is bound by instruction issue, so its issue rate against the SMs'
 # peak (4 schedulers x 1 instruction per cycle) is the bound that applies.
-K_LAYERS_WARP_INST_PER_POINT = 96.5
+K_LAYERS_WARP_INST_PER_POINT = 96.55
+# Where the two figures come from (reported with them in the JSON line).
+K_LAYERS_CAPTURE = {"commit": "e6a809f", "summary": "profiles/k_layers_uneven256.md",
+                    "workload": "256-event uneven batch, 13,628,373 points, both passes"}
 
 
 
@@ -588,6 +591,7 @@ def run_gb300(args):
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
     issue_peak = props.multi_processor_count * 4 * mhz * 1e6
     issue_achieved = K_LAYERS_WARP_INST_PER_POINT * N / (layers_ms / 1000.0)
+    roofline["traffic_source"] = K_LAYERS_CAPTURE
     roofline["issue"] = {"warp_instructions_per_point": K_LAYERS_WARP_INST_PER_POINT,
                          "achieved_warp_inst_per_s": issue_achieved, "peak_warp_inst_per_s": issue_peak,
                          "frac": issue_achieved / issue_peak, "sm_mhz": mhz}
