@@ -1,7 +1,8 @@
 """ctypes front end of the oracle (test infrastructure, not product code).
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
-use this package, as the checker (and bench.py to time the CPU baseline).
+use this package: to check the CUDA path's results (and bench.py to time
+the CPU baseline).
 ``clue2d``/``clue3d`` run the CPU restatement (oracle/clue_oracle.c);
 ``ref_clue2d``/``ref_clue2d_batch``/``ref_clue3d`` run the unmodified
 reference serial code when oracle/_ref was built (from the reference tree or
