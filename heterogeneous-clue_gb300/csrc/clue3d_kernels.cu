@@ -346,18 +346,28 @@ __device__ __forceinline__ void visit_row_masked(const V& v, int r, const ColMas
 // row's mask in one uniform pass and then visiting only the rows whose bit is
 // set keeps the lanes of a warp together: otherwise each of the ~25 rows would
 // send the few lanes with an entry down the visit while the others wait.
-// Windows of more than 8 layers return false (the caller loops directly).
+// Windows of more than 8 layers or 5 eta rows return false (the caller loops
+// directly).
 template <class V>
 __device__ __forceinline__ bool live_rows(const V& v, int lo, int hi, int skip, int e0, int e1, const ColMask& wm,
                                           unsigned long long* live) {
-  if (hi - lo >= 8) return false;
+  if (hi - lo >= 8 || e1 - e0 >= 5) return false;
   unsigned long long m = 0;
+  const int ne = e1 - e0;
   for (int cl = lo; cl <= hi; ++cl) {
     if (cl == skip) continue;
-    for (int ie = e0; ie <= e1; ++ie) {
-      const ulonglong2 rm = v.mm(cl * kEtaBins + ie);
-      if ((rm.x & wm.w0) | (rm.y & wm.w1)) m |= 1ull << ((cl - lo) * 8 + (ie - e0));
+    // a layer's (at most five) window rows are consecutive: their masks are
+    // read together and their bits set with one shift
+    const int r0 = cl * kEtaBins + e0;
+    unsigned bits = 0;
+#pragma unroll
+    for (int de = 0; de < 5; ++de) {
+      if (de <= ne) {
+        const ulonglong2 rm = v.mm(r0 + de);
+        bits |= (((rm.x & wm.w0) | (rm.y & wm.w1)) != 0ull ? 1u : 0u) << de;
+      }
     }
+    m |= (unsigned long long)bits << ((cl - lo) * 8);
   }
   *live = m;
   return true;
