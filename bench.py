@@ -51,13 +51,13 @@ PARAMS = (1.3, 2.0, 2.0)
 # DRAM bytes per point of k_layers (both passes of one batch), from an ncu capture
 # of the 256-event uneven batch (dram read + write over its 13,628,373 points);
 # traffic grows with the point count, so a full launch is scaled by its points.
-K_LAYERS_DRAM_BYTES_PER_POINT = 24.50
+K_LAYERS_DRAM_BYTES_PER_POINT = 24.44
 # Warp instructions per point of k_layers (both passes), same capture: the
 # kernel is bound by instruction issue, so its issue rate against the SMs'
 # peak (4 schedulers x 1 instruction per cycle) is the bound that applies.
-K_LAYERS_WARP_INST_PER_POINT = 96.55
+K_LAYERS_WARP_INST_PER_POINT = 96.99
 # Where the two figures come from (reported with them in the JSON line).
-K_LAYERS_CAPTURE = {"commit": "e6a809f", "summary": "profiles/k_layers_uneven256.md",
+K_LAYERS_CAPTURE = {"commit": "ab43302", "summary": "profiles/k_layers_uneven256.md",
                     "workload": "256-event uneven batch, 13,628,373 points, both passes"}
 
 
