@@ -15,8 +15,10 @@
 //   k3_key        flat key per cluster; clusters per (event, row) and each
 //                 cluster's arrival slot in its row
 //   k3_row_scan   per event: first position of each row
-//   k3_scatter    place clusters into their rows (arrival order)
-//   k3_row_sort   order each row by (phi bin, index)
+//   k3_scatter    place clusters into their rows (arrival order) with their
+//                 candidate and query records; row occupancy masks
+//   k3_row_sort   order each row by (phi bin, index): a counting sort by
+//                 column through the mask, or a count where a column repeats
 //   k3_search<true>   KernelCalculateDensitySoA (:26-150), one block per
 //                     (event, slab of layers) with the slab's rows staged
 //   k3_search<false>  KernelComputeDistanceToHigherSoA (:286-392), likewise
@@ -473,7 +475,8 @@ __device__ __forceinline__ void search_live(const V& v, const Params3D& P, const
 // layers).  The block copies the rows of the slab's layers and of the
 // sibling layers around them (occupancy masks, row starts, phi columns and
 // the 16-byte candidate records) into shared memory once, then runs the
-// searches of the slab's clusters from there.  A cluster whose window leaves
+// searches of the slab's clusters from there (4 blocks of 256 threads per SM;
+// slabs of 2, 6 and 8 layers measured slower or the same).  A cluster whose window leaves
 // the staged rows (the phi bin 126 quirk can move a cluster into the next
 // layer's first row) and a slab larger than the staging area read the global
 // arrays instead; either way the visiting order and arithmetic are the
