@@ -187,6 +187,8 @@ __global__ void k3_scatter(Batch3D b, Params3D P) {
     const int pbin = k - li * kBins - eb * kPhiBins;
     const int bins = li | (eb << 11) | (pbin << 17);
     b.tqrec[pos] = make_float4(zi, __fmul_rn(roa, zi), thr, __int_as_float(bins));
+  } else {
+    b.tqrec[pos] = make_float4(0.f, 0.f, 0.f, 0.f);  // the junk row's entries are never queried
   }
   unsigned long long* m = b.row_mask + 2 * r;
   const unsigned long long bit = 1ull << (col & 63);
@@ -222,7 +224,7 @@ __global__ void k3_row_sort(Batch3D b) {
   b.sorted[f] = idx;
   b.scol[f] = col;
   b.cand[f] = b.tcand[p];
-  b.qrec[f] = b.tqrec[p];  // rejected clusters (the junk row) carry no query record
+  b.qrec[f] = b.tqrec[p];
 }
 
 // The rows of one event as the searches see them: the whole event in global
@@ -381,22 +383,32 @@ struct Query3 {
   int li, eb, pb, self;   // self: the cluster's own position in the view
 };
 
-// Density terms of one row of a query's window (KernelCalculateDensitySoA,
-// :26-150): the clusters of the row in the window's phi columns, in order.
+// One density term (KernelCalculateDensitySoA, :26-150): candidate q of a
+// row of layer cl, in the reference's operation order.
+template <class V>
+__device__ __forceinline__ void density_term(const V& v, const Params3D& P, const Query3& Q, float coef, int q,
+                                             float& rho) {
+  const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
+  const float r1 = __fmul_rn(cj.x, Q.z);
+  const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
+  const float d0 = __fsub_rn(Q.r0, r1);
+  const float a = __fmul_rn(d0, d0);
+  const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
+  if (__fadd_rn(a, c) < Q.aux) rho = __fadd_rn(rho, __fmul_rn((q == Q.self) ? 1.f : coef, cj.z));
+}
+
+__device__ __forceinline__ float density_coef(const Params3D& P, const Query3& Q, int cl) {
+  return __fmul_rn(P.kdf, (cl == Q.li && !P.dens_same) ? 0.f : 1.f);
+}
+
+// Density terms of one row of a query's window: the clusters of the row in
+// the window's phi columns, in order.
 template <class V>
 __device__ __forceinline__ void density_row(const V& v, const Params3D& P, const Query3& Q, const ColMask& wm, int cl,
                                             int ie, float& rho) {
-  const bool same = (cl == Q.li);
-  const float coef = __fmul_rn(P.kdf, (same && !P.dens_same) ? 0.f : 1.f);
-  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 2, Q.pb + 2, [&](int q) {
-    const float4 cj = v.rec(q);  // {roa, phi, energy, -}; q == self is the cluster itself
-    const float r1 = __fmul_rn(cj.x, Q.z);
-    const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
-    const float d0 = __fsub_rn(Q.r0, r1);
-    const float a = __fmul_rn(d0, d0);
-    const float c = __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi);
-    if (__fadd_rn(a, c) < Q.aux) rho = __fadd_rn(rho, __fmul_rn((q == Q.self) ? 1.f : coef, cj.z));
-  });
+  const float coef = density_coef(P, Q, cl);
+  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 2, Q.pb + 2,
+                   [&](int q) { density_term(v, P, Q, coef, q, rho); });
 }
 
 // One cluster's nearest higher (KernelComputeDistanceToHigherSoA, :286-392)
@@ -408,22 +420,75 @@ struct Nh3 {
 };
 
 template <class V>
+__device__ __forceinline__ void nh_term(const V& v, const Params3D& P, const Query3& Q, int cl, int q, Nh3& o) {
+  const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
+  const float r1 = __fmul_rn(cj.x, Q.z);
+  const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
+  const float d0 = __fsub_rn(Q.r0, r1);
+  const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
+  if (cj.w > Q.aux && d <= o.best) {  // "<=": the last candidate wins a tie
+    o.best = d;
+    o.best_t = __fsqrt_rn(d);
+    o.best_l = abs(cl - Q.li);
+    o.nl = cl;
+    o.nq = q;
+  }
+}
+
+template <class V>
 __device__ __forceinline__ void nh_row(const V& v, const Params3D& P, const Query3& Q, const ColMask& wm, int cl, int ie,
                                        Nh3& o) {
-  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 1, Q.pb + 1, [&](int q) {
-    const float4 cj = v.rec(q);  // {roa, phi, energy, rho}
-    const float r1 = __fmul_rn(cj.x, Q.z);
-    const float dphi = reduce_range(__fsub_rn(Q.phi, cj.y), P);
-    const float d0 = __fsub_rn(Q.r0, r1);
-    const float d = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(__fmul_rn(__fmul_rn(r1, r1), dphi), dphi));
-    if (cj.w > Q.aux && d <= o.best) {  // "<=": the last candidate wins a tie
-      o.best = d;
-      o.best_t = __fsqrt_rn(d);
-      o.best_l = abs(cl - Q.li);
-      o.nl = cl;
-      o.nq = q;
+  visit_row_masked(v, cl * kEtaBins + ie, wm, Q.pb - 1, Q.pb + 1, [&](int q) { nh_term(v, P, Q, cl, q, o); });
+}
+
+// The window's phi columns as visited: arc A = [a0, a1] first, then arc B =
+// [0, b1] when the window wraps (b1 = -1 otherwise); lt = the columns below
+// a0.  All of a window's columns at or above a0 are arc A.
+struct Arcs {
+  unsigned long long lt0, lt1;
+  int a0, a1, b1;
+  __device__ __forceinline__ Arcs(int p0, int p1) {
+    if (p0 < 0) {
+      a0 = p0 + kPhiBins; a1 = kPhiBins - 1; b1 = p1;
+    } else if (p1 >= kPhiBins) {
+      a0 = p0; a1 = kPhiBins - 1; b1 = p1 - kPhiBins;
+    } else {
+      a0 = p0; a1 = p1; b1 = -1;
     }
-  });
+    lt0 = a0 >= 64 ? ~0ull : ((1ull << a0) - 1);
+    lt1 = a0 > 64 ? ((1ull << (a0 - 64)) - 1) : 0ull;
+  }
+};
+
+// A live row's entries in the window, in the reference's order, with one
+// code path for every lane: the run of arc A starts after the row's entries
+// below a0 and the run of arc B at the row's start; without a repeated
+// column both come from popcounts of the row mask, with one the row's
+// columns are counted (rows are short).
+template <class V, class F>
+__device__ __forceinline__ void visit_live(const V& v, int r, const ColMask& wm, const Arcs& ar, F&& f) {
+  const ulonglong2 m = v.mm(r);
+  const int s = v.start(r);
+  int qa, na, nb;
+  if (!(m.y >> 63)) {
+    const unsigned long long x0 = m.x & wm.w0, x1 = m.y & wm.w1;  // entries in the window
+    na = __popcll(x0 & ~ar.lt0) + __popcll(x1 & ~ar.lt1);
+    nb = __popcll(x0) + __popcll(x1) - na;
+    qa = s + __popcll(m.x & ar.lt0) + __popcll(m.y & ar.lt1);
+  } else {
+    const int t = v.start(r + 1);
+    int below = 0;
+    na = nb = 0;
+    for (int q = s; q < t; ++q) {
+      const int c = v.col(q);
+      below += c < ar.a0;
+      na += (c >= ar.a0) & (c <= ar.a1);
+      nb += c <= ar.b1;
+    }
+    qa = s + below;
+  }
+  for (int q = qa; q < qa + na; ++q) f(q);
+  for (int q = s; q < s + nb; ++q) f(q);
 }
 
 // The window of a query: layers [lo, hi] (without `skip`), eta rows
@@ -462,12 +527,19 @@ template <bool kDensity, class V, class R>
 __device__ __forceinline__ void search_live(const V& v, const Params3D& P, const Query3& Q, unsigned long long live,
                                             R& res) {
   const Window3 w = window_of(P, Q, kDensity);
-  const ColMask wm(Q.pb, kDensity ? 2 : 1);
+  const int d = kDensity ? 2 : 1;
+  const ColMask wm(Q.pb, d);
+  const Arcs ar(Q.pb - d, Q.pb + d);
   while (live) {
     const int k = __ffsll((long long)live) - 1;
     live &= live - 1;
-    if constexpr (kDensity) density_row(v, P, Q, wm, w.lo + (k >> 3), w.e0 + (k & 7), res);
-    else nh_row(v, P, Q, wm, w.lo + (k >> 3), w.e0 + (k & 7), res);
+    const int cl = w.lo + (k >> 3), r = cl * kEtaBins + w.e0 + (k & 7);
+    if constexpr (kDensity) {
+      const float coef = density_coef(P, Q, cl);
+      visit_live(v, r, wm, ar, [&](int q) { density_term(v, P, Q, coef, q, res); });
+    } else {
+      visit_live(v, r, wm, ar, [&](int q) { nh_term(v, P, Q, cl, q, res); });
+    }
   }
 }
 
