@@ -16,7 +16,7 @@
 //                 cluster's arrival slot in its row
 //   k3_row_scan   per event: first position of each row
 //   k3_scatter    place clusters into their rows (arrival order) with their
-//                 candidate and query records; row occupancy masks
+//                 candidate and query records; row occupancy and repeat masks
 //   k3_row_sort   order each row by (phi bin, index): a counting sort by
 //                 column through the mask, or a count where a column repeats
 //   k3_search<true>   KernelCalculateDensitySoA (:26-150), one block per
@@ -192,7 +192,13 @@ __global__ void k3_scatter(Batch3D b, Params3D P) {
   }
   unsigned long long* m = b.row_mask + 2 * r;
   const unsigned long long bit = 1ull << (col & 63);
-  if (atomicOr(m + (col >> 6), bit) & bit) atomicOr(m + 1, 1ull << 63);
+  if (atomicOr(m + (col >> 6), bit) & bit) {
+    atomicOr(m + 1, 1ull << 63);
+    // a second entry in the column: the column's bit in the repeat mask; a
+    // third: bit 127 of the repeat mask
+    unsigned long long* rp = b.row_rep + 2 * r;
+    if (atomicOr(rp + (col >> 6), bit) & bit) atomicOr(rp + 1, 1ull << 63);
+  }
 }
 
 // Each entry's rank inside its row by (column, index) gives its final slot:
@@ -244,6 +250,7 @@ struct RowsGlobal {
 
 struct RowsStaged {
   const unsigned long long* mask;  // 2 words per staged row
+  const unsigned long long* rmask; // 2 words per staged row: columns holding two entries; bit 127: three or more
   const int32_t* rstart;           // relative to the first staged entry
   const float4* cand;
   const uint8_t* scol;
@@ -252,6 +259,9 @@ struct RowsStaged {
   __device__ __forceinline__ unsigned long long m1(int r) const { return mask[2 * (r - row_lo) + 1]; }
   __device__ __forceinline__ ulonglong2 mm(int r) const {
     return reinterpret_cast<const ulonglong2*>(mask)[r - row_lo];
+  }
+  __device__ __forceinline__ ulonglong2 rep(int r) const {
+    return reinterpret_cast<const ulonglong2*>(rmask)[r - row_lo];
   }
   __device__ __forceinline__ int start(int r) const { return rstart[r - row_lo]; }
   __device__ __forceinline__ float4 rec(int q) const { return cand[q]; }
@@ -462,19 +472,23 @@ struct Arcs {
 
 // A live row's entries in the window, in the reference's order, with one
 // code path for every lane: the run of arc A starts after the row's entries
-// below a0 and the run of arc B at the row's start; without a repeated
-// column both come from popcounts of the row mask, with one the row's
-// columns are counted (rows are short).
-template <class V, class F>
-__device__ __forceinline__ void visit_live(const V& v, int r, const ColMask& wm, const Arcs& ar, F&& f) {
+// below a0 and the run of arc B at the row's start.  The counts come from
+// popcounts of the row mask plus, where a column holds two entries, of the
+// repeat mask; only a row with three or more entries in one column is
+// counted entry by entry (rows are short).
+template <class F>
+__device__ __forceinline__ void visit_live(const RowsStaged& v, int r, const ColMask& wm, const Arcs& ar, F&& f) {
   const ulonglong2 m = v.mm(r);
   const int s = v.start(r);
+  ulonglong2 rp = make_ulonglong2(0ull, 0ull);
+  if (m.y >> 63) rp = v.rep(r);
   int qa, na, nb;
-  if (!(m.y >> 63)) {
-    const unsigned long long x0 = m.x & wm.w0, x1 = m.y & wm.w1;  // entries in the window
-    na = __popcll(x0 & ~ar.lt0) + __popcll(x1 & ~ar.lt1);
-    nb = __popcll(x0) + __popcll(x1) - na;
-    qa = s + __popcll(m.x & ar.lt0) + __popcll(m.y & ar.lt1);
+  if (!(rp.y >> 63)) {
+    const unsigned long long x0 = m.x & wm.w0, x1 = m.y & wm.w1;    // columns in the window
+    const unsigned long long y0 = rp.x & wm.w0, y1 = rp.y & wm.w1;  // ... holding a second entry
+    na = __popcll(x0 & ~ar.lt0) + __popcll(x1 & ~ar.lt1) + __popcll(y0 & ~ar.lt0) + __popcll(y1 & ~ar.lt1);
+    nb = __popcll(x0) + __popcll(x1) + __popcll(y0) + __popcll(y1) - na;
+    qa = s + __popcll(m.x & ar.lt0) + __popcll(m.y & ar.lt1) + __popcll(rp.x & ar.lt0) + __popcll(rp.y & ar.lt1);
   } else {
     const int t = v.start(r + 1);
     int below = 0;
@@ -523,9 +537,9 @@ __device__ __forceinline__ void search_all(const V& v, const Params3D& P, const 
 }
 
 // The same search over the rows named by a live_rows() mask.
-template <bool kDensity, class V, class R>
-__device__ __forceinline__ void search_live(const V& v, const Params3D& P, const Query3& Q, unsigned long long live,
-                                            R& res) {
+template <bool kDensity, class R>
+__device__ __forceinline__ void search_live(const RowsStaged& v, const Params3D& P, const Query3& Q,
+                                            unsigned long long live, R& res) {
   const Window3 w = window_of(P, Q, kDensity);
   const int d = kDensity ? 2 : 1;
   const ColMask wm(Q.pb, d);
@@ -555,17 +569,19 @@ __device__ __forceinline__ void search_live(const V& v, const Params3D& P, const
 // reference's.
 constexpr int kSlabLayers = 4;
 constexpr int kSlabThreads = 256;
-constexpr int kSlabMaxRows = 512;
+constexpr int kSlabMaxRows = 384;  // 10 layers of rows and one more: sibling windows up to +-3 layers
 constexpr int kSlabMaxCand = 2048;
-constexpr size_t kSlabSmem = 16 * (size_t)kSlabMaxRows + 4 * (size_t)(kSlabMaxRows + 1) +
+constexpr size_t kSlabSmem = 32 * (size_t)kSlabMaxRows + 4 * (size_t)(kSlabMaxRows + 1) +
                              16 * (size_t)kSlabMaxCand + (size_t)kSlabMaxCand;
+static_assert(kSlabSmem <= 48 * 1024, "static shared memory");
 
 template <bool kDensity>
 __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D P, int n_slabs) {
   __shared__ __align__(16) unsigned char sm3[kSlabSmem];
   unsigned long long* s_mask = reinterpret_cast<unsigned long long*>(sm3);
-  float4* s_cand = reinterpret_cast<float4*>(sm3 + 16 * (size_t)kSlabMaxRows);
-  int32_t* s_rs = reinterpret_cast<int32_t*>(sm3 + 16 * (size_t)kSlabMaxRows + 16 * (size_t)kSlabMaxCand);
+  unsigned long long* s_rep = s_mask + 2 * kSlabMaxRows;
+  float4* s_cand = reinterpret_cast<float4*>(sm3 + 32 * (size_t)kSlabMaxRows);
+  int32_t* s_rs = reinterpret_cast<int32_t*>(sm3 + 32 * (size_t)kSlabMaxRows + 16 * (size_t)kSlabMaxCand);
   uint8_t* s_col = reinterpret_cast<uint8_t*>(s_rs + kSlabMaxRows + 1);
   const int e = blockIdx.x / n_slabs;
   const int L0 = (blockIdx.x % n_slabs) * kSlabLayers;
@@ -585,7 +601,11 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
   const bool staged = nrows <= kSlabMaxRows && pos_hi - pos_lo <= kSlabMaxCand;
   if (staged) {
     const unsigned long long* gm = b.row_mask + 2 * (rbase + row_lo);
-    for (int i = threadIdx.x; i < 2 * nrows; i += kSlabThreads) s_mask[i] = gm[i];
+    const unsigned long long* gr = b.row_rep + 2 * (rbase + row_lo);
+    for (int i = threadIdx.x; i < 2 * nrows; i += kSlabThreads) {
+      s_mask[i] = gm[i];
+      s_rep[i] = gr[i];
+    }
     for (int i = threadIdx.x; i <= nrows; i += kSlabThreads) s_rs[i] = rs[row_lo + i] - pos_lo;
     for (int i = threadIdx.x; i < pos_hi - pos_lo; i += kSlabThreads) {
       s_cand[i] = b.cand[pos_lo + i];
@@ -593,7 +613,7 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
     }
     __syncthreads();
   }
-  RowsStaged sv{s_mask, s_rs, s_cand, s_col, row_lo};
+  RowsStaged sv{s_mask, s_rep, s_rs, s_cand, s_col, row_lo};
   RowsGlobal gv{b.row_mask + 2 * rbase, rs, b.cand, b.scol};
   const int64_t es = b.offsets[e];
   const int tid = threadIdx.x;
@@ -740,6 +760,8 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   cudaError_t err = cudaMemsetAsync(b.row_cnt, 0, sizeof(int32_t) * (size_t)b.n_events * b.n_rows, s);
   if (err != cudaSuccess) return err;
   err = cudaMemsetAsync(b.row_mask, 0, 16 * (size_t)b.n_events * b.n_rows, s);
+  if (err != cudaSuccess) return err;
+  err = cudaMemsetAsync(b.row_rep, 0, 16 * (size_t)b.n_events * b.n_rows, s);
   if (err != cudaSuccess) return err;
   const int T = 256;
   const int grid = (int)((b.n_points + T - 1) / T);

@@ -45,7 +45,7 @@ Params3D make_params3d(const clue3d_params& q) {
 }
 
 enum Slot3D : int {
-  T_OFF, T_KEY, T_RCNT, T_RSTART, T_ARR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_CAND, T_QREC, T_TCAND, T_TQREC,
+  T_OFF, T_KEY, T_RCNT, T_RSTART, T_ARR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_REP, T_CAND, T_QREC, T_TCAND, T_TQREC,
   T_IN0, T_IN1, T_IN2, T_IN3, T_IN4, T_IN5, T_IN6, T_IN7,
   T_OUT0, T_OUT1, T_OUT2, T_OUT3, T_OUT4, T_OUT5, T_OUT6,
   T_COUNT
@@ -116,7 +116,7 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     need[T_RSTART] = 4 * (size_t)(E * n_rows + 1);
     need[T_EVSEEDS] = 4 * (size_t)E;
     need[T_FLAGS] = 4 * kFlagCount;
-    need[T_MASK] = 16 * (size_t)(E * n_rows);
+    need[T_MASK] = need[T_REP] = 16 * (size_t)(E * n_rows);
     need[T_CAND] = need[T_QREC] = need[T_TCAND] = need[T_TQREC] = 16 * (size_t)N;
     if (host_io) {
       for (int s = T_IN0; s <= T_OUT6; ++s) need[s] = 4 * (size_t)N;
@@ -180,6 +180,7 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     b.ev_seeds = static_cast<int32_t*>(P(T_EVSEEDS));
     b.flags = static_cast<int32_t*>(P(T_FLAGS));
     b.row_mask = static_cast<unsigned long long*>(P(T_MASK));
+    b.row_rep = static_cast<unsigned long long*>(P(T_REP));
     b.cand = static_cast<float4*>(P(T_CAND));
     b.qrec = static_cast<float4*>(P(T_QREC));
     b.tcand = static_cast<float4*>(P(T_TCAND));

@@ -179,6 +179,7 @@ struct Batch3D {
   int32_t* par = nullptr;      // [N]
   int32_t* ev_seeds = nullptr; // [E] tracksters per event
   unsigned long long* row_mask = nullptr;  // [E * n_rows * 2] phi columns present in each row; bit 127: a column repeats
+  unsigned long long* row_rep = nullptr;   // [E * n_rows * 2] columns holding a second entry; bit 127: a third
   int32_t* flags = nullptr;    // [kFlagCount]
 };
 
