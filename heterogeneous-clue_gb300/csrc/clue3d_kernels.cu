@@ -470,39 +470,40 @@ struct Arcs {
   }
 };
 
-// A live row's entries in the window, in the reference's order, with one
-// code path for every lane: the run of arc A starts after the row's entries
-// below a0 and the run of arc B at the row's start.  The counts come from
-// popcounts of the row mask plus, where a column holds two entries, of the
-// repeat mask; only a row with three or more entries in one column is
-// counted entry by entry (rows are short).
-template <class F>
-__device__ __forceinline__ void visit_live(const RowsStaged& v, int r, const ColMask& wm, const Arcs& ar, F&& f) {
+// A live row's entries in the window, in the reference's order: the run of
+// arc A, [qa, qa + na), then the run of arc B, [s, s + nb) (the row's start).
+// The counts come from popcounts of the row mask plus, where a column holds
+// two entries, of the repeat mask; only a row with three or more entries in
+// one column is counted entry by entry (rows are short).
+struct RowRuns {
+  int qa, na, s, nb;
+};
+
+__device__ __forceinline__ RowRuns row_runs(const RowsStaged& v, int r, const ColMask& wm, const Arcs& ar) {
   const ulonglong2 m = v.mm(r);
-  const int s = v.start(r);
+  RowRuns o;
+  o.s = v.start(r);
   ulonglong2 rp = make_ulonglong2(0ull, 0ull);
   if (m.y >> 63) rp = v.rep(r);
-  int qa, na, nb;
   if (!(rp.y >> 63)) {
     const unsigned long long x0 = m.x & wm.w0, x1 = m.y & wm.w1;    // columns in the window
     const unsigned long long y0 = rp.x & wm.w0, y1 = rp.y & wm.w1;  // ... holding a second entry
-    na = __popcll(x0 & ~ar.lt0) + __popcll(x1 & ~ar.lt1) + __popcll(y0 & ~ar.lt0) + __popcll(y1 & ~ar.lt1);
-    nb = __popcll(x0) + __popcll(x1) + __popcll(y0) + __popcll(y1) - na;
-    qa = s + __popcll(m.x & ar.lt0) + __popcll(m.y & ar.lt1) + __popcll(rp.x & ar.lt0) + __popcll(rp.y & ar.lt1);
+    o.na = __popcll(x0 & ~ar.lt0) + __popcll(x1 & ~ar.lt1) + __popcll(y0 & ~ar.lt0) + __popcll(y1 & ~ar.lt1);
+    o.nb = __popcll(x0) + __popcll(x1) + __popcll(y0) + __popcll(y1) - o.na;
+    o.qa = o.s + __popcll(m.x & ar.lt0) + __popcll(m.y & ar.lt1) + __popcll(rp.x & ar.lt0) + __popcll(rp.y & ar.lt1);
   } else {
     const int t = v.start(r + 1);
     int below = 0;
-    na = nb = 0;
-    for (int q = s; q < t; ++q) {
+    o.na = o.nb = 0;
+    for (int q = o.s; q < t; ++q) {
       const int c = v.col(q);
       below += c < ar.a0;
-      na += (c >= ar.a0) & (c <= ar.a1);
-      nb += c <= ar.b1;
+      o.na += (c >= ar.a0) & (c <= ar.a1);
+      o.nb += c <= ar.b1;
     }
-    qa = s + below;
+    o.qa = o.s + below;
   }
-  for (int q = qa; q < qa + na; ++q) f(q);
-  for (int q = s; q < s + nb; ++q) f(q);
+  return o;
 }
 
 // The window of a query: layers [lo, hi] (without `skip`), eta rows
@@ -544,16 +545,37 @@ __device__ __forceinline__ void search_live(const RowsStaged& v, const Params3D&
   const int d = kDensity ? 2 : 1;
   const ColMask wm(Q.pb, d);
   const Arcs ar(Q.pb - d, Q.pb + d);
-  while (live) {
-    const int k = __ffsll((long long)live) - 1;
-    live &= live - 1;
-    const int cl = w.lo + (k >> 3), r = cl * kEtaBins + w.e0 + (k & 7);
-    if constexpr (kDensity) {
-      const float coef = density_coef(P, Q, cl);
-      visit_live(v, r, wm, ar, [&](int q) { density_term(v, P, Q, coef, q, res); });
-    } else {
-      visit_live(v, r, wm, ar, [&](int q) { nh_term(v, P, Q, cl, q, res); });
+  // One candidate per iteration: the lanes of a warp step through their own
+  // candidate sequences together, and a lane moves to its next run (arc B of
+  // the row, or the next live row) only when its current run is done.
+  int q = 0, qe = 0, qb = 0, qbe = 0, cl = 0;
+  float coef = 0.f;
+  bool more = true;
+  for (;;) {
+    while (q >= qe) {
+      if (qb < qbe) {
+        q = qb;
+        qe = qbe;
+        qb = qbe = 0;
+      } else if (live) {
+        const int k = __ffsll((long long)live) - 1;
+        live &= live - 1;
+        cl = w.lo + (k >> 3);
+        if constexpr (kDensity) coef = density_coef(P, Q, cl);
+        const RowRuns rr = row_runs(v, cl * kEtaBins + w.e0 + (k & 7), wm, ar);
+        q = rr.qa;
+        qe = rr.qa + rr.na;
+        qb = rr.s;
+        qbe = rr.s + rr.nb;
+      } else {
+        more = false;
+        break;
+      }
     }
+    if (!more) break;
+    if constexpr (kDensity) density_term(v, P, Q, coef, q, res);
+    else nh_term(v, P, Q, cl, q, res);
+    ++q;
   }
 }
 
