@@ -41,14 +41,14 @@ constexpr int kEtaBins = 34;
 constexpr int kPhiBins = 126;
 constexpr int kBins = kEtaBins * kPhiBins;
 
-__device__ __forceinline__ int event_of(const int64_t* off, int n_events, int64_t i) {
-  int lo = 0, hi = n_events;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (off[mid] <= i) lo = mid; else hi = mid;
-  }
-  return lo;
+// Event of cluster i: from the event of its 256-cluster block's first
+// cluster, forward past the events that end at or before i.
+__device__ __forceinline__ int event_of_blk(const Batch3D& b, int64_t i) {
+  int e = b.blk_ev[i >> 8];
+  while (b.offsets[e + 1] <= i) ++e;
+  return e;
 }
+
 
 // reco::reduceRange for float (src/serial/DataFormats/Math/deltaPhi.h:16-23)
 __device__ __forceinline__ float reduce_range(float x, const Params3D& P) {
@@ -97,7 +97,7 @@ __global__ void k3_key(Batch3D b, Params3D P) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int row = -1, e = 0;
   if (i < b.n_points) {
-    e = event_of(b.offsets, b.n_events, i);
+    e = event_of_blk(b, i);
     const int l = b.layer[i];
     const int pb = phi_bin(b.phi[i], P);
     int k = -1;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k3_row_scan(Batch3D b) {
 __global__ void k3_scatter(Batch3D b, Params3D P) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= b.n_points) return;
-  const int e = event_of(b.offsets, b.n_events, i);
+  const int e = event_of_blk(b, i);
   const int k = b.key[i];
   const int row = row_of(k, b.n_rows);
   const int64_t r = (int64_t)e * b.n_rows + row;
@@ -209,7 +209,7 @@ __global__ void k3_scatter(Batch3D b, Params3D P) {
 __global__ void k3_row_sort(Batch3D b) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= b.n_points) return;
-  const int e = event_of(b.offsets, b.n_events, p);
+  const int e = event_of_blk(b, p);
   const int idx = b.tmp[p], cr = b.par[p];
   const int col = cr & 127;
   const int64_t r = (int64_t)e * b.n_rows + (cr >> 7);

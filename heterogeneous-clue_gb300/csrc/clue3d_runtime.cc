@@ -45,7 +45,7 @@ Params3D make_params3d(const clue3d_params& q) {
 }
 
 enum Slot3D : int {
-  T_OFF, T_KEY, T_RCNT, T_RSTART, T_ARR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_REP, T_CAND, T_QREC, T_TCAND, T_TQREC,
+  T_OFF, T_BEV, T_KEY, T_RCNT, T_RSTART, T_ARR, T_SORTED, T_SCOL, T_TMP, T_PAR, T_EVSEEDS, T_FLAGS, T_MASK, T_REP, T_CAND, T_QREC, T_TCAND, T_TQREC,
   T_IN0, T_IN1, T_IN2, T_IN3, T_IN4, T_IN5, T_IN6, T_IN7,
   T_OUT0, T_OUT1, T_OUT2, T_OUT3, T_OUT4, T_OUT5, T_OUT6,
   T_COUNT
@@ -111,6 +111,8 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     const bool host_io = !(flags & CLUE_DEVICE_MEMORY);
     std::vector<size_t> need(T_COUNT, 0);
     need[T_OFF] = 8 * (size_t)(E + 1);
+    const int64_t n_blk = (N + 255) / 256;
+    need[T_BEV] = 4 * (size_t)n_blk;
     need[T_KEY] = need[T_ARR] = need[T_SORTED] = need[T_SCOL] = need[T_TMP] = need[T_PAR] = 4 * (size_t)N;
     need[T_RCNT] = 4 * (size_t)(E * n_rows);
     need[T_RSTART] = 4 * (size_t)(E * n_rows + 1);
@@ -123,13 +125,20 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     }
     rc = h->arena3d.reserve(need, h->budget > h->arena.total() ? h->budget - h->arena.total() : 0);
     if (rc) return rc;
-    rc = h->stage.reserve(8 * (size_t)(E + 1));
+    rc = h->stage.reserve(8 * (size_t)(E + 1) + 4 * (size_t)n_blk);
     if (rc) return rc;
     rc = h->flags_host.reserve(4 * kFlagCount);
     if (rc) return rc;
     rc = h->nt_host.reserve(4 * (size_t)E);
     if (rc) return rc;
     memcpy(h->stage.p, off, 8 * (size_t)(E + 1));
+    // the event of each 256-cluster block's first cluster, so that a kernel
+    // finds a cluster's event in a step or two instead of a binary search
+    int32_t* bev = reinterpret_cast<int32_t*>(static_cast<char*>(h->stage.p) + 8 * (size_t)(E + 1));
+    for (int64_t j = 0, ev = 0; j < n_blk; ++j) {
+      while (off[ev + 1] <= 256 * j) ++ev;
+      bev[j] = (int32_t)ev;
+    }
 
     auto P = [&](int s) { return h->arena3d.ptr(s); };
     cudaStream_t s = h->stream;
@@ -142,8 +151,10 @@ int clue3d_run_batch(clue_handle* hh, const clue3d_params* prm, int32_t E, const
     void* dout[7];
     const size_t n4 = 4 * (size_t)N;
     if ((e = cudaMemsetAsync(P(T_FLAGS), 0, 4 * kFlagCount, s)) != cudaSuccess) return cuda_error(e, "memset");
-    if ((e = cudaMemcpyAsync(P(T_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(P(T_OFF), h->stage.p, 8 * (size_t)(E + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P(T_BEV), bev, 4 * (size_t)n_blk, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_error(e, "H2D offsets");
+    b.blk_ev = static_cast<const int32_t*>(P(T_BEV));
     for (int i = 0; i < 8; ++i) {
       if (host_io) {
         din[i] = P(T_IN0 + i);

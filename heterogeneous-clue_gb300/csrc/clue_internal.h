@@ -149,6 +149,7 @@ struct Batch3D {
   int64_t n_points = 0;
   int32_t n_rows = 0;  // rows (layer, eta) per event: n_layers * 34 + 1
   const int64_t* offsets = nullptr;  // [E+1]
+  const int32_t* blk_ev = nullptr;   // [ceil(N / 256)] event of each 256-cluster block's first cluster
   const float* z = nullptr;
   const float* eta = nullptr;
   const float* phi = nullptr;
