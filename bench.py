@@ -382,28 +382,35 @@ def config2_leg(C, torch, stream, args):
         algo.autotune(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out,
                       cache_path=os.path.join(tempfile.gettempdir(), "clue_gb300_autotune.jsonl"))
 
-    def run(flags):
-        algo.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
+    def run(h, flags):
+        h.run_batch(off, dev["x"], dev["y"], dev["layer"], dev["weight"], out=out, flags=C.DEVICE_MEMORY | flags)
 
-    def timed(flags, warm, steps):
+    def timed(h, flags, warm, steps):
         """Per-step times (ms, CUDA events on the stream) of ``steps`` steps after ``warm``."""
         for _ in range(warm):
-            run(flags)
+            run(h, flags)
         torch.cuda.synchronize()
         ts = []
         for _ in range(steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            run(flags)
+            run(h, flags)
             e1.record(stream)
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1))
-        algo.synchronize()
+        h.synchronize()
         return ts
 
     steps = max(5, args.steps)
-    tb = timed(0, 3, steps)
-    tp = timed(C.PLAIN, 2, steps)
+    tb = timed(algo, 0, 3, steps)
+    # the plain form on a handle of its own with the same tuning: on the handle
+    # the autotuner ran on, one-event runs measured up to 1.5x slower
+    plain_h = C.Clusterizer(*PARAMS, budget_bytes=96 << 30, stream=stream.cuda_stream)
+    t = algo.get_tuning()
+    plain_h.set_tuning(threads=t["threads"], layer_capacity=t["layer_capacity"], big_threads=t["big_threads"],
+                       big_capacity=t["big_capacity"])
+    tp = timed(plain_h, C.PLAIN, 2, steps)
+    plain_h.close()
     ms_b, ms_p = statistics.median(tb), statistics.median(tp)
     tuning = algo.get_tuning()
     chain = None if args.no_chain else chain_leg(C, torch, stream, algo, off, dev, out, steps)
