@@ -21,8 +21,8 @@
 //                 column through the mask, or a count where a column repeats
 //   k3_search<true>   KernelCalculateDensitySoA (:26-150), one block per
 //                     (event, slab of layers) with the slab's rows staged
-//   k3_search<false>  KernelComputeDistanceToHigherSoA (:286-392), likewise
-//   k3_flags      seeds, outliers, parent pointers (:509-560)
+//   k3_search<false>  KernelComputeDistanceToHigherSoA (:286-392), likewise,
+//                     then seeds, outliers and parent pointers (:509-560)
 //   k3_finish     per event: trackster ids by seed rank, pointer jumping
 //                 along nearestHigher, labels (:564-577)
 // Float arithmetic uses explicit _rn intrinsics in the reference's operation
@@ -109,6 +109,7 @@ __global__ void k3_key(Batch3D b, Params3D P) {
       k = l * kBins + pb + eta_bin(b.eta[i], P) * kPhiBins;
     }
     b.key[i] = k;
+    if (k < 0) b.seed[i] = -1;  // not searched: k3_finish makes it a root of its own
     row = row_of(k, b.n_rows);
   }
   const int gkey = row >= 0 ? e * b.n_rows + row : -1;
@@ -162,7 +163,8 @@ __global__ void __launch_bounds__(256) k3_row_scan(Batch3D b) {
 // and the searches need of it, read here in input order (coalesced): its
 // event-local index, phi column and row; its 16-byte candidate record {roa,
 // phi, energy, rho} (rho added by the density search); its 16-byte query
-// record {z, roa * z, density threshold, layer | etaBin << 11 | phiBin << 17}.
+// record {z, roa * z, density threshold, layer | etaBin << 11 | phiBin << 17 |
+// isSilicon << 24}.
 // The cluster also goes into its row's 128-bit phi-column occupancy mask;
 // bit 127 marks a column held twice.
 __global__ void k3_scatter(Batch3D b, Params3D P) {
@@ -185,7 +187,7 @@ __global__ void k3_scatter(Batch3D b, Params3D P) {
     // phiBin up to 126), without k3_key's double-precision product again
     const int li = b.layer[i], eb = eta_bin(b.eta[i], P);
     const int pbin = k - li * kBins - eb * kPhiBins;
-    const int bins = li | (eb << 11) | (pbin << 17);
+    const int bins = li | (eb << 11) | (pbin << 17) | ((b.sil[i] ? 1 : 0) << 24);
     b.tqrec[pos] = make_float4(zi, __fmul_rn(roa, zi), thr, __int_as_float(bins));
   } else {
     b.tqrec[pos] = make_float4(0.f, 0.f, 0.f, 0.f);  // the junk row's entries are never queried
@@ -391,6 +393,8 @@ __device__ __forceinline__ bool live_rows(const V& v, int lo, int hi, int skip, 
 struct Query3 {
   float phi, z, r0, aux;  // aux: density threshold (density), rho (nearest higher)
   int li, eb, pb, self;   // self: the cluster's own position in the view
+  float energy;
+  bool sil;
 };
 
 // One density term (KernelCalculateDensitySoA, :26-150): candidate q of a
@@ -648,7 +652,9 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
     Query3 Q;
     Q.li = bins & 0x7ff;
     Q.eb = (bins >> 11) & 0x3f;
-    Q.pb = bins >> 17;
+    Q.pb = (bins >> 17) & 0x7f;
+    Q.sil = (bins >> 24) & 1;
+    Q.energy = cr.z;
     Q.phi = cr.y;
     Q.z = qr.x;
     Q.r0 = qr.y;
@@ -683,39 +689,27 @@ __global__ void __launch_bounds__(kSlabThreads, 4) k3_search(Batch3D b, Params3D
       else if (inside) search_all<false>(sv, P, Q, o);
       else search_all<false>(gv, P, Q, o);
       if (o.nq >= 0 && inside) o.nq += pos_lo;
-      if (o.best != FLT_MAX) {
-        b.delta_t[gi] = o.best_t;
-        b.delta_l[gi] = o.best_l;
-        b.nh_l[gi] = o.nl;
-        b.nh_i[gi] = b.sorted[o.nq];
-      } else {
-        b.delta_t[gi] = FLT_MAX;
-        b.delta_l[gi] = INT_MAX;
-        b.nh_l[gi] = -1;
-        b.nh_i[gi] = -1;
-      }
+      const bool found = o.best != FLT_MAX;
+      const float dt = found ? o.best_t : FLT_MAX;
+      const int dl = found ? o.best_l : INT_MAX, nl = found ? o.nl : -1;
+      const int ni = found ? b.sorted[o.nq] : -1;
+      b.delta_t[gi] = dt;
+      b.delta_l[gi] = dl;
+      b.nh_l[gi] = nl;
+      b.nh_i[gi] = ni;
+      // seeds and outliers (CLUE3DAlgoKernels.h:521-560); par: the nearest
+      // higher for followers, -2 for seeds, -3 for other roots
+      const float r = Q.aux;
+      const float dxy = Q.sil ? P.crit_xy : b.radius[gi];
+      const bool seed = (dt > dxy || __int2float_rn(dl) > P.crit_z) && (r >= P.crit_rho) &&
+                        (__fdiv_rn(Q.energy, r) > P.crit_self);
+      const bool outlier = (dt > P.out_thr) && (r < P.crit_rho);
+      b.seed[gi] = seed ? 1 : 0;
+      b.par[gi] = seed ? -2 : ((!outlier && nl >= 0) ? ni : -3);
     }
   }
 }
 
-// Seeds and outliers (CLUE3DAlgoKernels.h:521-560).  par: nearest higher for
-// followers, -2 for seeds, -3 for other roots.
-__global__ void k3_flags(Batch3D b, Params3D P) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= b.n_points) return;
-  if (b.key[i] < 0) {
-    b.seed[i] = 0;
-    b.par[i] = -3;
-    return;
-  }
-  const float dt = b.delta_t[i], r = b.rho[i];
-  const float dxy = b.sil[i] ? P.crit_xy : b.radius[i];
-  const bool seed = (dt > dxy || __int2float_rn(b.delta_l[i]) > P.crit_z) && (r >= P.crit_rho) &&
-                    (__fdiv_rn(b.energy[i], r) > P.crit_self);
-  const bool outlier = (dt > P.out_thr) && (r < P.crit_rho);
-  b.seed[i] = seed ? 1 : 0;
-  b.par[i] = seed ? -2 : ((!outlier && b.nh_l[i] >= 0) ? b.nh_i[i] : -3);
-}
 
 // One block per event: trackster ids by seed rank in index order, then
 // pointer jumping along nearestHigher (replaces the LIFO propagation), then
@@ -726,7 +720,7 @@ __global__ void __launch_bounds__(512) k3_finish(Batch3D b) {
   const int n = (int)(b.offsets[e + 1] - es);
   int32_t* par = b.par + es;
   int32_t* ti = b.ti + es;
-  const int32_t* seed = b.seed + es;
+  int32_t* seed = b.seed + es;
   __shared__ int s_w[16];
   __shared__ int s_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -734,7 +728,12 @@ __global__ void __launch_bounds__(512) k3_finish(Batch3D b) {
   __syncthreads();
   for (int base = 0; base < n; base += 512) {
     const int i = base + threadIdx.x;
-    const int f = (i < n) ? seed[i] : 0;
+    int f = (i < n) ? seed[i] : 0;
+    if (f < 0) {  // rejected by k3_key: no seed, a root of its own
+      f = 0;
+      seed[i] = 0;
+      par[i] = -3;
+    }
     int x = f;
     for (int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, x, o);
@@ -813,10 +812,6 @@ cudaError_t launch_clue3d(const Batch3D& b, const Params3D& p, cudaStream_t s) {
   {
     NvtxRange r("clue3d/nearest_higher");
     k3_search<false><<<(unsigned)slab_blocks, kSlabThreads, 0, s>>>(b, p, n_slabs);
-  }
-  {
-    NvtxRange r("clue3d/flags");
-    k3_flags<<<grid, T, 0, s>>>(b, p);
   }
   {
     NvtxRange r("clue3d/finish");
